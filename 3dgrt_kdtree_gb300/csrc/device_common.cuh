@@ -1,0 +1,99 @@
+// device_common.cuh -- types shared by the render kernels and the host API.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kdgr.h"
+
+namespace kdgr {
+
+// CameraInfo of the reference (cudaRenderer.cu:336): eye, right/up axes,
+// top-left point of the near-plane window and the per-pixel steps.
+struct CamInfo {
+  float eye[3], u[3], v[3], start[3];
+  float step_x, step_y;
+};
+
+// The host camera set-up of renderGaussianWithCudaFrame
+// (cudaRenderer.cu:3112-3127) in the reference's types and order.
+CamInfo make_caminfo(const kdgr_camera& cam, int width, int height);
+
+// Device arrays of the oracle-matching (plain drop-in) form.
+//   nodes:   the reference's 8-byte nodes, in the file's order;
+//   offsets: leaf Gaussian-ID lists;
+//   test:    4 x float4 per Gaussian, the fields the ray-Gaussian test reads:
+//            (pos.xyz, opacity) (1/s.xyz, s.x) (s.y, s.z, q.w, q.x) (q.y, q.z, 0, 0)
+//            with 1/s the reference's uploaded (inverted) scale and s its
+//            IEEE reciprocal, the value rayPrimIntersect computes per call;
+//   sh:      12 x float4 per Gaussian, coefficient-major RGB (k*3 + c).
+struct ExactView {
+  const uint2* nodes;
+  const uint32_t* offsets;
+  const float4* test;
+  const float4* sh;
+  uint32_t n_nodes, n_offsets, n_gauss;
+  float bmin[3], bmax[3];
+};
+
+// Device arrays of the fast forms.
+//   nodes:   re-laid-out tree: the top `top_nodes` nodes in breadth-first
+//            order (staged in shared memory), the rest depth-first by subtree;
+//            children stay pairwise adjacent.  Leaf words are unchanged.
+//   test:    4 x float4 per Gaussian: rows of M = diag(1/s) R^T with
+//            b = M mu folded in: (M0, b0) (M1, b1) (M2, b2) (opacity, 0, 0, 0).
+//   sh:      FP32 coefficient-major (shared with ExactView) or, packed, BF16.
+//   packed:  2 x float4 per Gaussian (pos.xyz f32 | half2 s.xy | half2 s.z,op |
+//            half2 q.wx | half2 q.yz | u32 aniso index or ~0u).
+//   aniso:   3 x float4 per anisotropic Gaussian: (M0,b0)(M1,b1)(M2,b2) from the
+//            FP64 upload-time precompute.
+struct FastView {
+  const uint2* nodes;
+  const uint32_t* offsets;
+  const float4* test;
+  const float4* sh;
+  const uint4* packed;
+  const uint4* sh_bf16;
+  const float4* aniso;
+  uint32_t n_nodes, n_offsets, n_gauss, top_nodes;
+  float bmin[3], bmax[3];
+};
+
+// One view of a batch: camera, image size, 8x4-pixel tile grid and where its
+// pixels go in the output buffers.
+struct ViewDesc {
+  CamInfo cam;
+  int32_t W, H;
+  uint32_t tiles_x;
+  uint32_t tile_base;  // first global tile of this view
+  uint64_t out_off;
+};
+
+__host__ __device__ inline uint64_t fnv_add(uint64_t h, uint32_t v) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    h ^= (v >> (8 * i)) & 0xFFu;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+constexpr uint64_t kFnvInit = 14695981039346656037ull;
+
+// Error bits a kernel writes to its status word (never traps).
+enum : uint32_t {
+  kStatusBadNode = 1u,     // child index outside the node array
+  kStatusBadLeaf = 2u,     // leaf range outside the ID array
+  kStatusBadId = 4u,       // Gaussian ID >= n_gauss
+  kStatusQueueTimeout = 8u, // a bounded queue wait expired
+  kStatusStepLimit = 16u    // a ray exceeded kMaxRaySteps node fetches
+};
+
+// Upper bound on node fetches per ray.  A valid tree needs far fewer (each
+// leaf is entered once per restart and restarts strictly advance t_near);
+// the bound only guarantees that a kernel on a malformed input ends.
+constexpr uint32_t kMaxRaySteps = 1u << 22;
+
+// Launch entry points (render_exact.cu).
+cudaError_t launch_exact(const ExactView& s, const CamInfo& cam, int width, int height, float* rgb, float* alpha,
+                         float* depth, kdgr_ray_trace* trace, uint32_t* status, int kbuf, cudaStream_t stream);
+
+}  // namespace kdgr

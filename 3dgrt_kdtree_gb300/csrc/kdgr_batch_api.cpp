@@ -1,0 +1,256 @@
+// kdgr_batch_api.cpp -- C ABI of the batching form: one-shot batches,
+// CUDA-graph-captured batches and the autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kdgr_internal.h"
+#include "scene.h"
+
+using namespace kdgr;
+
+struct kdgr_batch_s {
+  kdgr_scene_t scene = nullptr;
+  kdgr_batch_config cfg{};
+  ViewDesc* d_views = nullptr;
+  uint32_t* d_queue = nullptr;
+  int n_views = 0;
+  uint32_t total_tiles = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int batch_args(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb, const kdgr_batch_config* cfg,
+               kdgr_batch_config& c, const char* who) {
+  if (!s || !views || n_views <= 0 || !rgb) {
+    set_error(std::string(who) + ": null scene/views/output or no views");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (cfg) c = *cfg;
+  else kdgr_batch_config_default(&c);
+  int rc = check_batch_config(s, c);
+  if (rc != KDGR_OK) set_error(std::string(who) + ": " + kdgr_last_error());
+  return rc;
+}
+
+// Stream-ordered scratch for one launch: view table + queue counter.
+int run_once(kdgr_scene_t s, const kdgr_batch_config& c, const std::vector<ViewDesc>& table, uint32_t total,
+             float* rgb, float* alpha, float* depth, cudaStream_t st, const char* who) {
+  const size_t vbytes = table.size() * sizeof(ViewDesc);
+  void* scratch = nullptr;
+  cudaError_t e = cudaMallocAsync(&scratch, vbytes + 256, st);
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  ViewDesc* d_views = static_cast<ViewDesc*>(scratch);
+  uint32_t* d_queue = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + ((vbytes + 127) & ~size_t(127)));
+  e = cudaMemcpyAsync(d_views, table.data(), vbytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, 4, st);
+  if (e == cudaSuccess) e = launch_batch(s, c, d_views, (int)table.size(), total, rgb, alpha, depth, d_queue, st);
+  const cudaError_t ef = cudaFreeAsync(scratch, st);
+  if (e == cudaSuccess) e = ef;
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  return KDGR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void kdgr_batch_config_default(kdgr_batch_config* c) {
+  if (!c) return;
+  c->kbuf = 8;
+  c->stack = 24;
+  c->blocks_per_sm = 0;
+  c->chunk = 4;
+  c->stage_top = 1;
+  c->precision = 0;
+}
+
+int kdgr_render_batch(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb, float* alpha, float* depth,
+                      const kdgr_batch_config* cfg, void* stream, float* ms_out) {
+  kdgr_batch_config c;
+  int rc = batch_args(s, views, n_views, rgb, cfg, c, "kdgr_render_batch");
+  if (rc != KDGR_OK) return rc;
+  std::vector<ViewDesc> table;
+  uint32_t total = 0;
+  rc = make_view_table(views, n_views, table, &total);
+  if (rc != KDGR_OK) return rc;
+  const cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (ms_out) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+  }
+  rc = run_once(s, c, table, total, rgb, alpha, depth, st, "kdgr_render_batch");
+  if (ms_out) {
+    cudaEventRecord(e1, st);
+    const cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    *ms_out = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == KDGR_OK && e != cudaSuccess) rc = cuda_fail(e, "kdgr_render_batch");
+  }
+  return rc;
+}
+
+int kdgr_render_fast(kdgr_scene_t s, const kdgr_camera* cam, int width, int height, float* rgb, float* alpha,
+                     float* depth, int precision, void* stream, float* ms_out) {
+  if (!cam) {
+    set_error("kdgr_render_fast: null camera");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  kdgr_view v;
+  v.cam = *cam;
+  v.width = width;
+  v.height = height;
+  v.out_offset = 0;
+  kdgr_batch_config c;
+  kdgr_batch_config_default(&c);
+  c.precision = precision ? 1 : 0;
+  return kdgr_render_batch(s, &v, 1, rgb, alpha, depth, &c, stream, ms_out);
+}
+
+int kdgr_batch_create(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb, float* alpha, float* depth,
+                      const kdgr_batch_config* cfg, kdgr_batch_t* out) {
+  if (!out) {
+    set_error("kdgr_batch_create: null output handle");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  kdgr_batch_config c;
+  int rc = batch_args(s, views, n_views, rgb, cfg, c, "kdgr_batch_create");
+  if (rc != KDGR_OK) return rc;
+  std::vector<ViewDesc> table;
+  uint32_t total = 0;
+  rc = make_view_table(views, n_views, table, &total);
+  if (rc != KDGR_OK) return rc;
+  kdgr_batch_s* b = new kdgr_batch_s;
+  b->scene = s;
+  b->cfg = c;
+  b->n_views = n_views;
+  b->total_tiles = total;
+  cudaStream_t cap = nullptr;
+  cudaError_t e = cudaMalloc(&b->d_views, table.size() * sizeof(ViewDesc));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, 4);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_views, table.data(), table.size() * sizeof(ViewDesc), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t le = cudaMemsetAsync(b->d_queue, 0, 4, cap);
+    if (le == cudaSuccess) le = launch_batch(s, c, b->d_views, n_views, total, rgb, alpha, depth, b->d_queue, cap);
+    e = cudaStreamEndCapture(cap, &b->graph);
+    if (e == cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  if (cap) cudaStreamDestroy(cap);
+  if (e != cudaSuccess) {
+    kdgr_batch_destroy(b);
+    return cuda_fail(e, "kdgr_batch_create");
+  }
+  *out = b;
+  return KDGR_OK;
+}
+
+int kdgr_batch_run(kdgr_batch_t b, void* stream) {
+  if (!b || !b->exec) {
+    set_error("kdgr_batch_run: invalid batch");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  cudaError_t e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "kdgr_batch_run");
+  return KDGR_OK;
+}
+
+int kdgr_batch_destroy(kdgr_batch_t b) {
+  if (!b) return KDGR_ERR_INVALID_ARG;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->d_views) cudaFree(b->d_views);
+  if (b->d_queue) cudaFree(b->d_queue);
+  delete b;
+  return KDGR_OK;
+}
+
+int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int precision, float* rgb,
+                  kdgr_batch_config* best, char* report, int report_len) {
+  if (!best) {
+    set_error("kdgr_autotune: null output config");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  kdgr_batch_config base;
+  int rc = batch_args(s, views, n_views, rgb, nullptr, base, "kdgr_autotune");
+  if (rc != KDGR_OK) return rc;
+  base.precision = precision ? 1 : 0;
+  rc = check_batch_config(s, base);
+  if (rc != KDGR_OK) return rc;
+  std::vector<ViewDesc> table;
+  uint32_t total = 0;
+  rc = make_view_table(views, n_views, table, &total);
+  if (rc != KDGR_OK) return rc;
+  std::vector<kdgr_batch_config> cands;
+  for (int kbuf : {8, 16})
+    for (int stack : {16, 24})
+      for (int chunk : {1, 4, 16})
+        for (int stage : {0, 1}) {
+          kdgr_batch_config c = base;
+          c.kbuf = kbuf;
+          c.stack = stack;
+          c.chunk = chunk;
+          c.stage_top = stage;
+          c.blocks_per_sm = 0;
+          cands.push_back(c);
+        }
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "kdgr_autotune");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  std::string rep;
+  float best_ms = 1e30f;
+  for (const kdgr_batch_config& c : cands) {
+    rc = run_once(s, c, table, total, rgb, nullptr, nullptr, st, "kdgr_autotune");  // warm-up
+    if (rc != KDGR_OK) break;
+    std::vector<float> ts;
+    for (int r = 0; r < 3 && rc == KDGR_OK; ++r) {
+      cudaEventRecord(e0, st);
+      rc = run_once(s, c, table, total, rgb, nullptr, nullptr, st, "kdgr_autotune");
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ts.push_back(ms);
+    }
+    if (rc != KDGR_OK) break;
+    std::sort(ts.begin(), ts.end());
+    const float med = ts[ts.size() / 2];
+    char line[256];
+    snprintf(line, sizeof(line),
+             "{\"kbuf\": %d, \"stack\": %d, \"chunk\": %d, \"stage_top\": %d, \"precision\": %d, \"ms\": %.4f}\n",
+             c.kbuf, c.stack, c.chunk, c.stage_top, c.precision, med);
+    rep += line;
+    if (med < best_ms) {
+      best_ms = med;
+      *best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  if (report && report_len > 0) {
+    strncpy(report, rep.c_str(), (size_t)report_len - 1);
+    report[report_len - 1] = '\0';
+  }
+  return rc;
+}
+
+}  // extern "C"

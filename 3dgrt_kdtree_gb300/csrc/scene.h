@@ -1,0 +1,80 @@
+// scene.h -- the scene handle behind kdgr_scene_t (host side).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "device_common.cuh"
+#include "kdgr.h"
+
+struct kdgr_scene_s {
+  int device = 0;
+  uint32_t forms = 0;  // KDGR_FORM_* materialised on the device
+  uint32_t n_nodes = 0, n_offsets = 0, n_gauss = 0;
+  uint32_t depth = 0, max_leaf = 0, n_leaves = 0;
+  float aabb[6] = {0, 0, 0, 0, 0, 0};  // .kdt order
+  // oracle-matching form
+  uint2* d_nodes = nullptr;
+  uint32_t* d_offsets = nullptr;
+  float4* d_test = nullptr;
+  float4* d_sh = nullptr;
+  // fast forms
+  uint2* d_nodes_fast = nullptr;
+  uint32_t top_nodes = 0;
+  float4* d_test_fast = nullptr;
+  uint4* d_packed = nullptr;
+  uint4* d_sh_bf16 = nullptr;
+  float4* d_aniso = nullptr;
+  uint32_t n_aniso = 0;
+  // per-scene status word written by kernels (error bits)
+  uint32_t* d_status = nullptr;
+  size_t device_bytes = 0;
+  std::mutex mu;
+
+  kdgr::ExactView exact_view() const;
+  kdgr::FastView fast_view() const;
+};
+
+namespace kdgr {
+// Allocation helper that records bytes and frees everything on failure.
+struct DevAlloc {
+  std::vector<void*> ptrs;
+  size_t bytes = 0;
+  cudaError_t err = cudaSuccess;
+  template <typename T>
+  T* alloc(size_t count) {
+    if (err != cudaSuccess) return nullptr;
+    void* p = nullptr;
+    const size_t b = count * sizeof(T) + 16;
+    err = cudaMalloc(&p, b);
+    if (err != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    bytes += b;
+    return static_cast<T*>(p);
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+int cuda_fail(cudaError_t e, const char* where);
+// Fast-form tree relayout: top levels breadth-first, rest depth-first.
+void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std::vector<uint32_t>& out,
+                   uint32_t* top_count);
+// Packed precision form: BF16 SH, FP16 inverse scales / quaternion /
+// opacity, and the FP64 upload-time factors of anisotropic Gaussians.
+int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh, DevAlloc& A);
+// Batched rendering (render_fast.cu).
+int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t* total_tiles);
+int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c);
+cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewDesc* d_views, int n_views,
+                         uint32_t total_tiles, float* rgb, float* alpha, float* depth, uint32_t* queue,
+                         cudaStream_t st);
+int batch_sms();
+// Scale ratio above which a Gaussian's factors come from the FP64 precompute.
+constexpr double kAnisoRatio = 1e3;
+}  // namespace kdgr

@@ -1,0 +1,247 @@
+/* kdgr.h -- C ABI of libkdgr, a GB300-native (sm_103a) implementation of the
+ * hybrid kd-tree Gaussian ray tracer of hydarlisk/3dgrt_kdtree.
+ *
+ * Paths below are relative to the reference's Kd-treeConverter_v0.9/
+ * Kd-treeConverter/ directory.  Every entry point names the reference
+ * interface it replaces.
+ *
+ * Conventions (all entry points):
+ *   - return a kdgr_status; KDGR_OK is 0, errors are positive and never exit
+ *     the process (the reference's CUDA_CHECK calls exit(), cudaRenderer.cu:25-31);
+ *     kdgr_last_error() gives the message of the calling thread's last error;
+ *   - plain pointers and sizes; device buffers are raw CUDA device pointers,
+ *     streams are cudaStream_t passed as void*; the caller owns every buffer;
+ *   - a scene handle may be used from several threads; calls on one handle
+ *     that write the same output buffers must be ordered by the caller.
+ */
+#ifndef KDGR_H_
+#define KDGR_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  KDGR_OK = 0,
+  KDGR_ERR_INVALID_ARG = 1,
+  KDGR_ERR_CUDA = 2,
+  KDGR_ERR_OUT_OF_MEMORY = 3,
+  KDGR_ERR_IO = 4,
+  KDGR_ERR_FORMAT = 5,    /* malformed tree or file */
+  KDGR_ERR_BUDGET = 6,    /* serving admission refused by the HBM budget */
+  KDGR_ERR_TIMEOUT = 7,   /* a bounded wait expired */
+  KDGR_ERR_NOT_INITIALIZED = 8,
+  KDGR_ERR_CANCELLED = 9,
+  KDGR_ERR_LIMIT = 10     /* a size beyond a fixed maximum */
+} kdgr_status;
+
+/* ---------------------------------------------------------------- camera */
+
+/* The fields of the reference's Camera (OpenGLStuffs.h:21-28) that the
+ * renderer reads: position, right (u), up (v) and back (n) axes, and the
+ * double-precision vertical field of view in degrees, aspect ratio and near
+ * plane.  The camera looks along -naxis. */
+typedef struct {
+  float pos[3];
+  float uaxis[3];
+  float vaxis[3];
+  float naxis[3];
+  double fovy;
+  double aspect;
+  double near_c;
+} kdgr_camera;
+
+/* ------------------------------------------------------------------ tree */
+
+/* Build parameters of the reference kd-tree builder (CLI -m/-f/-i/-s/-sc,
+ * Kd-treeConverterMain.cpp:3679-3733; defaults of the render benchmark). */
+typedef struct {
+  int32_t max_level;    /* MAX_LEVEL (24) */
+  int32_t force_split;  /* FORCE_SPLIT_THRESHOLD in triangles (16); 0 = off */
+  float isect_cost;     /* ISCET_COST (5.0) */
+  int32_t sah_mode;     /* SAH_MODE: 0, 1 (default), 4 or 7 */
+  float sort_cost;      /* SORT_COST (0.5), used by SAH_MODE 7 */
+  int32_t threads;      /* host threads; 0 = all */
+} kdgr_build_params;
+
+/* A kd-tree in the reference's flat layout (KdTreeNode, Kd-treeConverter.h:
+ * 282-296,402-410): nodes[2*i] = x, nodes[2*i+1] = y.  Inner: x = child<<3 |
+ * axis, y = split bits; children at child and child+1.  Leaf: x = count<<3 |
+ * 3, y = offset into offsets[].  aabb is in .kdt order (xmin, ymin, zmin,
+ * xmax, ymax, zmax).  Arrays are malloc'd by the library: kdgr_tree_free. */
+typedef struct {
+  uint32_t* nodes;
+  uint32_t n_nodes;
+  uint32_t* offsets;
+  uint32_t n_offsets;
+  float aabb[6];
+  uint32_t depth;
+  uint32_t n_leaves;
+  uint32_t max_leaf;
+  uint8_t* valid;        /* per Gaussian: 1 if it has proxy triangles (built trees) */
+  uint32_t n_gaussians;  /* 0 for trees read from a file */
+} kdgr_tree;
+
+typedef struct {
+  double proxy_s;
+  double build_s;
+  uint64_t n_triangles;
+  uint32_t n_valid;
+} kdgr_build_stats;
+
+void kdgr_build_params_default(kdgr_build_params* params);
+
+/* Proxy-mesh + SAH kd-tree build over activated Gaussians (64-float records,
+ * the reference's Gaussian layout, scales NOT inverted).  Same tree, bit for
+ * bit, as build_kd_tree_for_composite_object (Kd-treeConverter.cpp:22) after
+ * create_composite_object_from_gaussians (Kd-treeConverterMain.cpp:1925). */
+int kdgr_build_tree(const float* gaussians, uint32_t n_gaussians, const kdgr_build_params* params,
+                    kdgr_tree* out, kdgr_build_stats* stats);
+
+/* read_kd_tree_from_file(obj, path, KD_TREE_DUMP_IN_BINARY)
+ * (Kd-treeConverter.cpp:444-495), with structural validation. */
+int kdgr_read_kdt(const char* path, kdgr_tree* out);
+
+/* dump_kd_tree_for_composite_object(obj, KD_TREE_DUMP_IN_BINARY, path, ...)
+ * (Kd-treeConverter.cpp:297-342). */
+int kdgr_write_kdt(const kdgr_tree* tree, const char* path);
+
+/* Child/leaf ranges in bounds, IDs < n_gaussians, no node reached twice. */
+int kdgr_validate_tree(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
+                       uint32_t n_gaussians);
+
+void kdgr_tree_free(kdgr_tree* tree);
+
+const char* kdgr_last_error(void);
+
+/* ------------------------------------------------------------ scenes */
+
+typedef struct kdgr_scene_s* kdgr_scene_t;
+
+/* kdgr_scene_create flags */
+#define KDGR_SCALES_INVERTED 0x1u /* scale[] holds 1/s already, as the reference's
+                                     caller leaves it (Kd-treeConverterMain.cpp:3636-3650) */
+#define KDGR_FORM_EXACT 0x10u     /* oracle-matching arrays (kdgr_render) */
+#define KDGR_FORM_FAST 0x20u      /* FP32 fast arrays (kdgr_render_fast, batches) */
+#define KDGR_FORM_PACKED 0x40u    /* BF16 SH + FP16 shape arrays (precision form) */
+/* flags without any KDGR_FORM_* bit materialise EXACT | FAST */
+
+typedef struct {
+  uint32_t n_nodes, n_offsets, n_gaussians;
+  uint32_t depth, n_leaves, max_leaf;
+  uint32_t forms;         /* KDGR_FORM_* present */
+  uint32_t top_nodes;     /* fast form: nodes staged in shared memory */
+  uint32_t n_aniso;       /* packed form: Gaussians with FP64-precomputed factors */
+  uint64_t device_bytes;  /* HBM held by the scene */
+} kdgr_scene_info;
+
+/* Select the device the calling thread uses (initCuda, cudaRenderer.cu:2445). */
+int kdgr_init(int device);
+/* Synchronise the device; scenes must be destroyed by the caller. */
+int kdgr_shutdown(void);
+
+/* renderGaussianWithCudaSetup (cudaRenderer.cu:2557-2703): upload a tree in
+ * the reference layout and activated Gaussians (64-float records, the
+ * reference's Gaussian struct).  Validates the tree first (KDGR_ERR_FORMAT). */
+int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
+                      const float aabb[6], const float* gaussians, uint32_t n_gaussians, uint32_t flags,
+                      kdgr_scene_t* out);
+/* cleanupCudaResources (cudaRenderer.cu) for one scene. */
+int kdgr_scene_destroy(kdgr_scene_t scene);
+int kdgr_scene_info_get(kdgr_scene_t scene, kdgr_scene_info* out);
+/* Error bits the kernels raised for this scene since the last clear
+ * (bounds violations; a bounded wait that expired).  Synchronises. */
+int kdgr_scene_status(kdgr_scene_t scene, uint32_t* bits, int clear);
+
+/* ------------------------------------------------------------ rendering */
+
+/* renderGaussianWithCudaFrame (cudaRenderer.cu:3099-3484), plain drop-in
+ * form: oracle-matching arithmetic, one launch per view.  Writes
+ * d_rgb[3*((H-1-y)*W + x) + c] (rows flipped, as the reference) and, when
+ * non-null, alpha and depth at the same pixel index.  With ms_out non-null
+ * the call waits for the kernel and returns its time (the reference returns
+ * FPS after an event sync); otherwise it is asynchronous on `stream`. */
+int kdgr_render(kdgr_scene_t scene, const kdgr_camera* cam, int width, int height, float* d_rgb, float* d_alpha,
+                float* d_depth, void* stream, float* ms_out);
+
+/* ------------------------------------------------------- batched rendering
+ * The batching, precision and serving forms.  One persistent launch draws
+ * 8x4-pixel ray tiles of every queued view from an atomic work queue.  These
+ * forms use fast FP32 arithmetic (FMA, rsqrt, exp2 approximation) and accept
+ * hits with t* in the half-open leaf interval [t_near, t_far); they agree
+ * with the FP64 oracle to <= 1e-3 RMSE.  No reference counterpart: the
+ * reference renders one view per launch (cudaRenderer.cu:3406). */
+typedef struct {
+  kdgr_camera cam;
+  int32_t width;
+  int32_t height;
+  uint64_t out_offset; /* first pixel of this view in the output buffers */
+} kdgr_view;
+
+typedef struct {
+  int32_t kbuf;          /* hit-buffer entries: 8 or 16 */
+  int32_t stack;         /* short-stack entries: 16 or 24 */
+  int32_t blocks_per_sm; /* persistent CTAs per SM; 0 = occupancy maximum */
+  int32_t chunk;         /* tiles a warp takes per queue operation (1..64) */
+  int32_t stage_top;     /* 1: stage the top tree levels in shared memory */
+  int32_t precision;     /* 0: FP32 arrays (KDGR_FORM_FAST); 1: BF16/FP16 arrays (KDGR_FORM_PACKED) */
+} kdgr_batch_config;
+
+void kdgr_batch_config_default(kdgr_batch_config* cfg);
+
+/* Render all views in one persistent launch.  Output pixel p of view v is at
+ * views[v].out_offset + (H-1-y)*W + x (rows flipped per view); rgb holds 3
+ * floats per pixel.  Scratch (view table, queue counter) is stream-ordered
+ * device memory taken and returned on `stream`.  ms_out as kdgr_render. */
+int kdgr_render_batch(kdgr_scene_t scene, const kdgr_view* views, int n_views, float* d_rgb, float* d_alpha,
+                      float* d_depth, const kdgr_batch_config* cfg, void* stream, float* ms_out);
+
+/* One view through the batch kernel with the default configuration;
+ * precision 0 = FP32 arrays, 1 = packed BF16/FP16 arrays. */
+int kdgr_render_fast(kdgr_scene_t scene, const kdgr_camera* cam, int width, int height, float* d_rgb,
+                     float* d_alpha, float* d_depth, int precision, void* stream, float* ms_out);
+
+/* A fixed batch captured once as a CUDA graph (queue reset + persistent
+ * launch) and replayed by kdgr_batch_run. */
+typedef struct kdgr_batch_s* kdgr_batch_t;
+int kdgr_batch_create(kdgr_scene_t scene, const kdgr_view* views, int n_views, float* d_rgb, float* d_alpha,
+                      float* d_depth, const kdgr_batch_config* cfg, kdgr_batch_t* out);
+int kdgr_batch_run(kdgr_batch_t batch, void* stream);
+int kdgr_batch_destroy(kdgr_batch_t batch);
+
+/* Time the kernel variants on the given views and return the fastest
+ * configuration (tile work per queue operation, hit-buffer and stack sizes,
+ * CTAs per SM, shared-memory staging).  d_rgb must hold the views' pixels.
+ * report (may be null) receives a JSON line per variant. */
+int kdgr_autotune(kdgr_scene_t scene, const kdgr_view* views, int n_views, int precision, float* d_rgb,
+                  kdgr_batch_config* best, char* report, int report_len);
+
+/* ------------------------------------------------------------ per-ray trace
+ * Written by the oracle-matching render path in trace mode (and by the CPU
+ * oracle) so the two can be compared ray by ray.  The counters are the
+ * reference's HIT_AND_NODE_COUNT_DEBUG quantities (cudaRenderer.cu:1504-1510,
+ * 1569-1606, 1679-1681); the hashes are 64-bit FNV-1a over the sequences. */
+typedef struct {
+  uint32_t n_inner;    /* inner-node descent steps */
+  uint32_t n_leaf;     /* leaves visited */
+  uint32_t n_cand;     /* candidates tested (sum of visited leaf sizes) */
+  uint32_t n_hit;      /* accepted hits the compositing loop reached */
+  uint32_t n_blend;    /* hits composited */
+  uint32_t n_restart;  /* restarts from the root after the short stack ran dry */
+  uint64_t h_leaf;     /* visited leaf node indices, in visit order */
+  uint64_t h_hit;      /* Gaussian IDs of reached hits, in compositing order */
+  uint64_t h_blend;    /* Gaussian IDs of composited hits, in order */
+} kdgr_ray_trace;
+
+/* kdgr_render plus one kdgr_ray_trace per pixel at d_trace[y*W + x] (kernel
+ * row order, not flipped).  Asynchronous on `stream`. */
+int kdgr_render_trace(kdgr_scene_t scene, const kdgr_camera* cam, int width, int height, float* d_rgb,
+                      float* d_alpha, float* d_depth, kdgr_ray_trace* d_trace, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KDGR_H_ */

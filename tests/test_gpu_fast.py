@@ -1,0 +1,112 @@
+"""Batching and precision forms against the FP64 oracle (<= 1e-3 RMSE),
+batch/graph/single-view equivalence, autotuner.  Through the C ABI."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import oracle_image
+
+pytestmark = pytest.mark.gpu
+
+RMSE_TOL = 1e-3  # the fast forms' accuracy bar against the FP64 oracle
+
+
+def fast_image(pkg, dev, scene, cam, W, H, precision=0):
+    rgb = torch.zeros(W * H * 3, device=dev)
+    alpha = torch.zeros(W * H, device=dev)
+    scene.render_fast(cam, W, H, rgb, alpha, precision=precision)
+    torch.cuda.synchronize()
+    assert scene.status() == 0
+    return rgb.cpu().numpy().reshape(H, W, 3), alpha.cpu().numpy().reshape(H, W)
+
+
+def rmse(a, b):
+    return float(np.sqrt(((a.astype(np.float64) - b) ** 2).mean()))
+
+
+@pytest.mark.parametrize("name", ["uniform2k", "cluster2k", "dense800"])
+def test_fast_forms_vs_fp64(pkg, O, cuda, fixtures, name):
+    fx = fixtures[name]
+    F = pkg.renderer
+    scene = F.Scene(fx.tree, fx.rec, forms=F.FORM_FAST | F.FORM_PACKED)
+    for _, cam, w, h, _ in fx.cameras():
+        r64, a64, _, _ = oracle_image(O, fx.tree, fx.rec, cam, w, h, precision="f64")
+        for prec in (0, 1):
+            rgb, a = fast_image(pkg, cuda, scene, cam, w, h, prec)
+            assert rmse(rgb, r64) <= RMSE_TOL, (prec, rmse(rgb, r64))
+            assert rmse(a, a64) <= RMSE_TOL
+    scene.close()
+
+
+def test_fast_forms_at_scale_vs_fp64(pkg, O, cuda):
+    """A 300k-Gaussian cluster+shell scene with the 5% anisotropic tail (some
+    Gaussians above scale ratio 1e3 take the FP64-precomputed factors)."""
+    sc = pkg.scenes
+    rec = sc.cluster_shell(300_000, seed=2, n_clusters=32)
+    tree = pkg.kdtree.build(rec)
+    F = pkg.renderer
+    scene = F.Scene(tree, rec, forms=F.FORM_FAST | F.FORM_PACKED)
+    n_aniso = scene.info()["n_aniso"]
+    assert n_aniso > 0 and abs(n_aniso - int((sc.scale_ratio(rec) > 1e3).sum())) <= 2
+    W, H = 320, 180
+    cam = sc.front_camera(W, H)
+    r64, _, _, _ = oracle_image(O, tree, rec, cam, W, H, precision="f64")
+    for prec in (0, 1):
+        rgb, _ = fast_image(pkg, cuda, scene, cam, W, H, prec)
+        assert rmse(rgb, r64) <= RMSE_TOL, (prec, rmse(rgb, r64))
+    scene.close()
+
+
+def test_batch_equals_single_views_and_graph(pkg, cuda, fixtures):
+    fx = fixtures["dense800"]
+    F = pkg.renderer
+    sc = pkg.scenes
+    scene = F.Scene(fx.tree, fx.rec)
+    cams = sc.sphere_cameras(6, seed=3, resolutions=[(40, 30), (64, 48), (17, 9)])
+    views, total, offs = F.make_views(cams)
+    rgb = torch.zeros(total * 3, device=cuda)
+    alpha = torch.zeros(total, device=cuda)
+    scene.render_batch(views, len(cams), rgb, alpha)
+    torch.cuda.synchronize()
+    batch = rgb.cpu().numpy().copy()
+    for (cam, w, h), off in zip(cams, offs):
+        single, _ = fast_image(pkg, cuda, scene, cam, w, h)
+        np.testing.assert_array_equal(batch[3 * off:3 * (off + w * h)].reshape(h, w, 3), single)
+    rgb2 = torch.zeros_like(rgb)
+    g = F.Batch(scene, views, len(cams), rgb2, None, None)
+    for _ in range(3):
+        g.run()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(rgb2.cpu().numpy(), batch)
+    g.close()
+    scene.close()
+
+
+def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
+    fx = fixtures["cluster2k"]
+    F = pkg.renderer
+    scene = F.Scene(fx.tree, fx.rec)
+    cams = pkg.scenes.sphere_cameras(4, seed=9, resolutions=[(64, 64)])
+    views, total, _ = F.make_views(cams)
+    rgb = torch.zeros(total * 3, device=cuda)
+    best, report = scene.autotune(views, len(cams), rgb)
+    assert best.kbuf in (8, 16) and best.stack in (16, 24) and best.chunk in (1, 4, 16)
+    assert len(report.strip().splitlines()) == 24
+    ref = torch.zeros_like(rgb)
+    scene.render_batch(views, len(cams), ref)
+    out = torch.zeros_like(rgb)
+    scene.render_batch(views, len(cams), out, cfg=best)
+    torch.cuda.synchronize()
+    assert float((out - ref).abs().max()) < 1e-4
+    scene.close()
+
+
+def test_batch_config_errors(pkg, cuda, fixtures):
+    fx = fixtures["uniform2k"]
+    F = pkg.renderer
+    scene = F.Scene(fx.tree, fx.rec, forms=F.FORM_EXACT)
+    views, total, _ = F.make_views(pkg.scenes.sphere_cameras(1, seed=1, resolutions=[(8, 8)]))
+    rgb = torch.zeros(total * 3, device=cuda)
+    with pytest.raises(pkg.capi.KdgrError):
+        scene.render_batch(views, 1, rgb)  # no fast arrays materialised
+    scene.close()

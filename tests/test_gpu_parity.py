@@ -1,0 +1,146 @@
+"""Plain drop-in kernel (oracle-matching form) against the CPU oracle, through
+the C ABI: per-ray visited-leaf and hit sequences bit-exact, RGB / alpha /
+depth bit-exact (the stated bar is 1e-5 absolute; the build meets it with
+zero difference)."""
+import numpy as np
+import pytest
+import torch
+
+import kat
+from gpu_util import flipped_index, gpu_exact, oracle_image
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_exact(g, o):
+    g_rgb, g_a, g_d, g_tr = g
+    o_rgb, o_a, o_d, o_tr = o
+    np.testing.assert_array_equal(g_tr, o_tr)
+    np.testing.assert_array_equal(g_rgb, o_rgb)
+    np.testing.assert_array_equal(g_a, o_a)
+    np.testing.assert_array_equal(g_d, o_d)
+
+
+@pytest.mark.parametrize("name", ["uniform2k", "cluster2k", "dense800"])
+def test_golden_scenes_bit_exact(pkg, O, cuda, fixtures, name):
+    fx = fixtures[name]
+    for cname, cam, w, h, words in fx.cameras():
+        g = gpu_exact(pkg, cuda, fx.tree, fx.rec, cam, w, h)
+        o = oracle_image(O, fx.tree, fx.rec, cam, w, h)
+        assert_exact(g, o)
+        ci = O.caminfo(cam, w, h)
+        same_cam = np.array_equal(
+            np.array(list(ci.eye) + list(ci.u) + list(ci.v) + list(ci.start) + [ci.step_x, ci.step_y],
+                     np.float32), words)
+        if same_cam:  # this host's tanf reproduces the committed camera words
+            np.testing.assert_array_equal(g[3], fx.out[f"{cname}_trace"])
+            np.testing.assert_array_equal(g[0], O.to_image(fx.out[f"{cname}_rgb"], w, h))
+
+
+@pytest.mark.parametrize("case", ["analytic", "straddle", "comb", "ties", "ties_perm", "big_leaf", "empty",
+                                  "miss"])
+def test_known_answer_scenes_bit_exact(pkg, O, cuda, case):
+    if case == "analytic":
+        tree, rec, cam = kat.analytic_single()
+        W, H = 32, 24
+    elif case == "straddle":
+        tree, _, rec, cam = kat.straddle()
+        W = H = 16
+    elif case == "comb":
+        tree, _, rec, cam = kat.comb(20)
+        W = H = 8
+    elif case == "ties":
+        tree, rec, cam = kat.ties(20)
+        W = H = 8
+    elif case == "ties_perm":
+        tree, rec, cam = kat.ties(20, [7, 3, 19, 0, 1, 2, 4, 6, 5, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18])
+        W = H = 8
+    elif case == "big_leaf":
+        tree, rec, cam = kat.big_leaf(100)
+        W = H = 16
+    elif case == "empty":
+        tree, rec, cam = kat.empty()
+        W = H = 8
+    else:
+        tree, rec, cam = kat.miss()
+        W = H = 8
+    g = gpu_exact(pkg, cuda, tree, rec, cam, W, H)
+    o = oracle_image(O, tree, rec, cam, W, H)
+    assert_exact(g, o)
+    if case == "comb":
+        assert g[3]["n_restart"].min() >= 1
+    if case == "big_leaf":
+        assert g[3]["n_hit"].max() > 16  # several passes of the 8-entry hit buffer
+
+
+@pytest.mark.parametrize("seed", [21, 22])
+def test_random_scenes_bit_exact(pkg, O, cuda, seed):
+    sc = pkg.scenes
+    rec = sc.uniform_cube(20000, seed=seed, scale=0.02) if seed % 2 else sc.cluster_shell(30000, seed=seed,
+                                                                                            n_clusters=12)
+    tree = pkg.kdtree.build(rec)
+    cam, W, H = sc.sphere_cameras(1, seed=seed, resolutions=[(96, 64)])[0]
+    assert_exact(gpu_exact(pkg, cuda, tree, rec, cam, W, H), oracle_image(O, tree, rec, cam, W, H))
+
+
+def test_uniform_100k_256_bit_exact(pkg, O, cuda):
+    """The small plain workload (100k Gaussians, 256x256) in full."""
+    sc = pkg.scenes
+    rec = sc.uniform_cube(100_000, seed=0)
+    tree = pkg.kdtree.build(rec)
+    cam = sc.front_camera(256, 256)
+    assert_exact(gpu_exact(pkg, cuda, tree, rec, cam, 256, 256), oracle_image(O, tree, rec, cam, 256, 256))
+
+
+def test_inverted_scale_flag_and_untraced_path(pkg, cuda, fixtures):
+    """The reference caller uploads 1/s (Kd-treeConverterMain.cpp:3636-3650);
+    both conventions and the untraced launch give identical images."""
+    import oracle as O
+    fx = fixtures["dense800"]
+    _, cam, w, h, _ = fx.cameras()[0]
+    a = gpu_exact(pkg, cuda, fx.tree, fx.rec, cam, w, h)
+    b = gpu_exact(pkg, cuda, fx.tree, O.invert_scales(fx.rec), cam, w, h, scales_inverted=True)
+    np.testing.assert_array_equal(a[0], b[0])
+    scene = pkg.renderer.Scene(fx.tree, fx.rec)
+    rgb = torch.zeros(w * h * 3, device=cuda)
+    ms = scene.render(cam, w, h, rgb, timed=True)
+    assert ms > 0
+    np.testing.assert_array_equal(rgb.cpu().numpy().reshape(h, w, 3), a[0])
+    scene.close()
+
+
+@pytest.fixture(scope="module")
+def cluster_1m(pkg):
+    """The at-scale workload: 1M-Gaussian cluster+shell scene and its tree."""
+    rec = pkg.scenes.cluster_shell(1_000_000, seed=1)
+    return rec, pkg.kdtree.build(rec)
+
+
+def test_1080p_1m_strided_rays_bit_exact(pkg, O, cuda, cluster_1m):
+    """Full-size parity: the plain kernel renders the whole 1920x1080 frame of
+    the 1M-Gaussian scene; every 97th ray is checked bit for bit against the
+    oracle (traces and colours)."""
+    rec, tree = cluster_1m
+    W, H = 1920, 1080
+    cam = pkg.scenes.front_camera(W, H)
+    g_rgb, g_a, g_d, g_tr = gpu_exact(pkg, cuda, tree, rec, cam, W, H)
+    pix = np.arange(0, W * H, 97, dtype=np.uint32)
+    o_rgb, o_a, o_d, o_tr = oracle_image(O, tree, rec, cam, W, H, pixels=pix)
+    fi = flipped_index(pix.astype(np.int64), W, H)
+    np.testing.assert_array_equal(g_tr[pix], o_tr)
+    np.testing.assert_array_equal(g_rgb.reshape(-1, 3)[fi], o_rgb)
+    np.testing.assert_array_equal(g_a.reshape(-1)[fi], o_a)
+    np.testing.assert_array_equal(g_d.reshape(-1)[fi], o_d)
+    # size-independent properties of the whole frame
+    assert np.isfinite(g_rgb).all() and (g_rgb >= 0).all()
+    assert (g_a >= 0).all() and (g_a <= 1.0).all()
+    assert (g_a > 0.99).mean() > 0.5
+
+
+def test_corrupt_tree_rejected_before_launch(pkg, cuda):
+    t = pkg.kdtree.KdTree(np.array([[(5 << 3) | 0, 0], [3, 0], [3, 0]], np.uint32), np.zeros(0, np.uint32),
+                          np.array([-1, -1, -1, 1, 1, 1], np.float32))
+    rec = np.stack([kat.gaussian((0, 0, 0), (0.1, 0.1, 0.1))])
+    with pytest.raises(pkg.capi.KdgrError) as e:
+        pkg.renderer.Scene(t, rec)
+    assert e.value.status == 5
