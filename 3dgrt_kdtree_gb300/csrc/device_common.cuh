@@ -39,32 +39,38 @@ struct ExactView {
 //   nodes:   re-laid-out tree: the top `top_nodes` nodes in breadth-first
 //            order (staged in shared memory), the rest depth-first by subtree;
 //            children stay pairwise adjacent.  Leaf words are unchanged.
-//   test:    4 x float4 per Gaussian: rows of M = diag(1/s) R^T with
-//            b = M mu folded in: (M0, b0) (M1, b1) (M2, b2) (opacity, 0, 0, 0).
-//   sh:      FP32 coefficient-major (shared with ExactView) or, packed, BF16.
-//   packed:  2 x float4 per Gaussian (pos.xyz f32 | half2 s.xy | half2 s.z,op |
-//            half2 q.wx | half2 q.yz | u32 aniso index or ~0u).
-//   aniso:   3 x float4 per anisotropic Gaussian: (M0,b0)(M1,b1)(M2,b2) from the
-//            FP64 upload-time precompute.
+//   test:    3 x float4 per Gaussian: rows of M = diag(1/s) R^T with
+//            b = M mu folded in: (M0, b0) (M1, b1) (M2, b2);
+//   opacity: 1 float per Gaussian;
+//   sh:      FP32 coefficient-major (shared with ExactView);
+//   packed:  2 x uint4 per Gaussian: (mu.xyz f32, opacity f32 with the sign
+//            bit set when the Gaussian is anisotropic) and (half2 1/s.xy,
+//            half2 1/s.z|0, half2 q.wx, half2 q.yz);
+//   sh_bf16: 6 x uint4 per Gaussian, BF16 coefficient-major;
+//   aniso_idx / aniso: for Gaussians with scale ratio > 1e3, the index into
+//            3 x float4 (M0,b0)(M1,b1)(M2,b2) from the FP64 upload precompute.
 struct FastView {
   const uint2* nodes;
   const uint32_t* offsets;
   const float4* test;
+  const float* opacity;
   const float4* sh;
   const uint4* packed;
   const uint4* sh_bf16;
+  const uint32_t* aniso_idx;
   const float4* aniso;
   uint32_t n_nodes, n_offsets, n_gauss, top_nodes;
   float bmin[3], bmax[3];
 };
 
-// One view of a batch: camera, image size, 8x4-pixel tile grid and where its
-// pixels go in the output buffers.
+// One view of a batch: camera, image size, its work-item grids and where its
+// pixels go in the output buffers.  Work items are 8x4-pixel warp tiles
+// (per-warp scheduling) or 16x8-pixel CTA blocks (per-CTA scheduling).
 struct ViewDesc {
   CamInfo cam;
   int32_t W, H;
-  uint32_t tiles_x;
-  uint32_t tile_base;  // first global tile of this view
+  uint32_t wt_x, wt_base;  // 8x4 tiles per row; first global tile of the view
+  uint32_t cb_x, cb_base;  // 16x8 blocks per row; first global block
   uint64_t out_off;
 };
 

@@ -8,6 +8,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -133,9 +134,11 @@ kdgr::FastView kdgr_scene_s::fast_view() const {
   v.nodes = d_nodes_fast;
   v.offsets = d_offsets;
   v.test = d_test_fast;
+  v.opacity = d_opacity;
   v.sh = d_sh;
   v.packed = d_packed;
   v.sh_bf16 = d_sh_bf16;
+  v.aniso_idx = d_aniso_idx;
   v.aniso = d_aniso;
   v.n_nodes = n_nodes;
   v.n_offsets = n_offsets;
@@ -285,12 +288,13 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
       return fail("kdgr_scene_create: upload (tree)");
   }
   if (forms & KDGR_FORM_FAST) {
-    std::vector<float> tf(16 * (size_t)n, 0.f);
+    std::vector<float> tf(12 * (size_t)n, 0.f), op(n);
     for (size_t i = 0; i < n; ++i) {
       const float* r = g + 64 * i;
       double m[3][3];
       quat_rt_d(r + 8, m);
-      float* t = tf.data() + 16 * i;
+      float* t = tf.data() + 12 * i;
+      op[i] = r[3];
       for (int row = 0; row < 3; ++row) {
         const double sc = giscl[3 * i + row];
         double b = 0;
@@ -301,11 +305,12 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
         }
         t[4 * row + 3] = (float)b;
       }
-      t[12] = r[3];
     }
-    s->d_test_fast = A.alloc<float4>(4 * (size_t)n);
+    s->d_test_fast = A.alloc<float4>(3 * (size_t)n);
+    s->d_opacity = A.alloc<float>(n);
     if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (fast)");
-    if (cudaMemcpy(s->d_test_fast, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+    if (cudaMemcpy(s->d_test_fast, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->d_opacity, op.data(), op.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
       return fail("kdgr_scene_create: upload (fast)");
   }
   if (forms & KDGR_FORM_PACKED) {
@@ -323,8 +328,9 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
 
 int kdgr_scene_destroy(kdgr_scene_t s) {
   if (!s) return KDGR_ERR_INVALID_ARG;
-  void* ps[] = {s->d_nodes, s->d_offsets, s->d_test, s->d_sh, s->d_nodes_fast, s->d_test_fast,
-                s->d_packed, s->d_sh_bf16, s->d_aniso, s->d_status};
+  void* ps[] = {s->d_nodes,  s->d_offsets, s->d_test,    s->d_sh,        s->d_nodes_fast, s->d_test_fast,
+                s->d_opacity, s->d_packed,  s->d_sh_bf16,   s->d_aniso_idx, s->d_aniso,
+                s->d_status};
   cudaError_t first = cudaSuccess;
   for (void* p : ps)
     if (p) {

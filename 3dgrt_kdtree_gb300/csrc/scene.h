@@ -25,8 +25,10 @@ struct kdgr_scene_s {
   uint2* d_nodes_fast = nullptr;
   uint32_t top_nodes = 0;
   float4* d_test_fast = nullptr;
+  float* d_opacity = nullptr;
   uint4* d_packed = nullptr;
   uint4* d_sh_bf16 = nullptr;
+  uint32_t* d_aniso_idx = nullptr;
   float4* d_aniso = nullptr;
   uint32_t n_aniso = 0;
   // per-scene status word written by kernels (error bits)
@@ -69,11 +71,12 @@ void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std:
 // opacity, and the FP64 upload-time factors of anisotropic Gaussians.
 int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh, DevAlloc& A);
 // Batched rendering (render_fast.cu).
-int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t* total_tiles);
+int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t* total_tiles,
+                    uint32_t* total_blocks);
 int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c);
 cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewDesc* d_views, int n_views,
-                         uint32_t total_tiles, float* rgb, float* alpha, float* depth, uint32_t* queue,
-                         cudaStream_t st);
+                         uint32_t total_tiles, uint32_t total_blocks, float* rgb, float* alpha, float* depth,
+                         uint32_t* queue, cudaStream_t st);
 int batch_sms();
 // Scale ratio above which a Gaussian's factors come from the FP64 precompute.
 constexpr double kAnisoRatio = 1e3;

@@ -41,7 +41,8 @@ class View(ctypes.Structure):
 
 class BatchConfig(ctypes.Structure):
     _fields_ = [("kbuf", ctypes.c_int32), ("stack", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("chunk", ctypes.c_int32), ("stage_top", ctypes.c_int32), ("precision", ctypes.c_int32)]
+                ("chunk", ctypes.c_int32), ("stage_top", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("cta_tiles", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

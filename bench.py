@@ -1,0 +1,382 @@
+"""Render benchmark: Mrays/s of the hybrid kd-tree Gaussian ray tracer.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config NAME] [--impl ours|reference]
+
+A step renders one batch of views of a resident scene.  Configurations:
+
+  scale     (default) 1M-Gaussian cluster+shell scene, one 1920x1080 view
+  small     100k Gaussians uniform in the unit cube, one 256x256 view
+  batching  the 1M scene, 64 views on spheres of radius 2-4 (16 each at
+            256x256, 640x480, 1280x720, 1920x1080) in one persistent launch
+  precision 3M Gaussians (256 clusters), 8 views at 1080p, BF16 SH and FP16
+            shape arrays with FP32 arithmetic
+
+`value` is the batched (persistent, CUDA-graph) form with the scene resident
+in HBM, timed with CUDA events per step with an L2 flush (a 512 MB write)
+between steps.  `e2e` is the same metric through the C ABI with host-side
+cameras and the frame read back into pinned host memory every step.
+`--impl reference` times the reference algorithm's CPU implementation (the
+oracle transcription of cudaRenderer.cu, all host threads) on a strided ray
+sample of the same workload.  Multi-GPU: scene replicas, no collective in
+the data path (views are independent), weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "Mrays/s at 1080p/1M Gaussians"
+UNIT = "Mrays/s"
+PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ workload
+def make_workload(pkg, name: str):
+    sc = pkg.scenes
+    if name == "small":
+        rec = sc.uniform_cube(100_000, seed=0)
+        cams = [(sc.front_camera(256, 256), 256, 256)]
+        desc = {"workload": "uniform cube, 100k Gaussians, 1 view 256x256", "gaussians": 100_000}
+    elif name == "scale":
+        rec = sc.cluster_shell(1_000_000, seed=1)
+        cams = [(sc.front_camera(1920, 1080), 1920, 1080)]
+        desc = {"workload": "cluster+shell, 1M Gaussians, 1 view 1920x1080", "gaussians": 1_000_000}
+    elif name == "mid":
+        rec = sc.cluster_shell(300_000, seed=1, n_clusters=64)
+        cams = [(sc.front_camera(1280, 720), 1280, 720)]
+        desc = {"workload": "cluster+shell, 300k Gaussians, 1 view 1280x720", "gaussians": 300_000}
+    elif name == "batching":
+        rec = sc.cluster_shell(1_000_000, seed=1)
+        cams = sc.sphere_cameras(64, seed=11)
+        desc = {"workload": "cluster+shell, 1M Gaussians, 64 mixed-resolution views", "gaussians": 1_000_000}
+    elif name == "precision":
+        rec = sc.cluster_shell(3_000_000, seed=2, n_clusters=256)
+        cams = sc.sphere_cameras(8, seed=12, resolutions=[(1920, 1080)], r_lo=2.5, r_hi=3.5)
+        desc = {"workload": "cluster+shell, 3M Gaussians, 8 views 1920x1080, BF16/FP16 storage",
+                "gaussians": 3_000_000}
+    else:
+        raise SystemExit(f"unknown config {name}")
+    desc["rays_per_step"] = int(sum(w * h for _, w, h in cams))
+    desc["views"] = len(cams)
+    return rec, cams, desc
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [l.split(",") for l in open(self.f.name).read().strip().splitlines() if l.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[0]) for r in rows if len(r) >= 8 and r[0].strip().replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if len(r) >= 8 and r[1].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 8 for i in range(4) if "Active" in r[4 + i]
+                          and "Not" not in r[4 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+def hbm_peak():
+    try:
+        return float(json.load(open(PEAKS))["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def algorithmic_bytes(tr, b_test: int, b_blend: int, b_out: int) -> float:
+    """Sum over rays of 8(N_inner+N_leaf) + 4 N_cand + b_test N_cand +
+    b_blend N_blend + b_out (counters of the oracle-matching kernel)."""
+    n = tr.shape[0]
+    return float(8 * (tr["n_inner"].sum(dtype=np.int64) + tr["n_leaf"].sum(dtype=np.int64))
+                 + (4 + b_test) * tr["n_cand"].sum(dtype=np.int64) + b_blend * tr["n_blend"].sum(dtype=np.int64)
+                 + b_out * n)
+
+
+def load_traffic():
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return {}
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, rank: int, world: int):
+    import torch
+    pkg = importlib.import_module("3dgrt_kdtree_gb300")
+    F = pkg.renderer
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    F.init(dev.index)
+    t0 = time.time()
+    rec, cams, desc = make_workload(pkg, args.config)
+    tree = pkg.kdtree.build(rec)
+    build_s = time.time() - t0
+    precision = 1 if args.config == "precision" else 0
+    forms = F.FORM_EXACT | (F.FORM_PACKED if precision else F.FORM_FAST)
+    scene = F.Scene(tree, rec, forms=forms)
+    info = scene.info()
+    log(f"[bench] {desc['workload']}: tree {tree.n_nodes} nodes, {tree.offsets.size} ids, depth {tree.depth}, "
+        f"built in {build_s:.1f}s; scene {info['device_bytes'] / 1e9:.2f} GB on device")
+    views, total_px, offs = F.make_views(cams)
+    rays = desc["rays_per_step"]
+    rgb = torch.zeros(total_px * 3, device=dev)
+    # autotuned persistent-kernel configuration
+    if args.profile:
+        cfg = F.BatchConfig.default()
+        cfg.precision = precision
+    else:
+        cfg, report = scene.autotune(views, len(cams), rgb, precision=precision)
+        log("[bench] autotuner variants:\n" + report.strip())
+        log(f"[bench] autotuner picked {cfg.as_dict()}")
+    batch = F.Batch(scene, views, len(cams), rgb, None, None, cfg)
+    flush = torch.empty((16 if args.profile else 512 * 1024 * 1024) // 4, dtype=torch.float32, device=dev)
+    if args.profile:
+        for _ in range(args.warmup + args.steps):
+            for (cam, w, h), off in zip(cams, offs):
+                scene.render(cam, w, h, rgb[3 * off:3 * (off + w * h)])
+        for _ in range(args.warmup + args.steps):
+            batch.run()
+        torch.cuda.synchronize(dev)
+        assert scene.status() == 0
+        print(json.dumps({"profile_run": args.config, "launches": args.warmup + args.steps}), flush=True)
+        raise SystemExit(0)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed_loop(step_fn, k):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        for i in range(k):
+            flush.zero_()
+            evs[i][0].record(stream)
+            step_fn()
+            evs[i][1].record(stream)
+        torch.cuda.synchronize(dev)
+        return [a.elapsed_time(b) for a, b in evs]
+
+    for _ in range(args.warmup):
+        batch.run()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(dev.index)
+    wall0 = time.time()
+    ms = timed_loop(batch.run, args.steps)
+    wall = time.time() - wall0
+    clk = clocks.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    assert scene.status() == 0, "kernel raised an error status"
+    ms_step = sum(ms) / len(ms)
+    if world > 1:
+        t = torch.tensor([ms_step], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = rays * world / (ms_step * 1e-3) / 1e6
+
+    # e2e: cameras from the host each step, frame read back into pinned memory
+    host = torch.empty(total_px * 3, dtype=torch.float32, pin_memory=True)
+
+    def e2e_step():
+        scene.render_batch(views, len(cams), rgb, cfg=cfg)
+        host.copy_(rgb, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    ms_e2e = timed_loop(e2e_step, args.steps)
+    e2e_step_ms = sum(ms_e2e) / len(ms_e2e)
+    view_bytes = 88 * len(cams)  # ViewDesc table (88 B per view) copied host->device by kdgr_render_batch
+    e2e = {"value": rays * world / (e2e_step_ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": view_bytes,
+           "d2h_bytes_per_step": int(host.numel() * 4), "ms_per_step": e2e_step_ms,
+           "path": "kdgr_render_batch (C ABI) + D2H of the RGB frame"}
+
+    # plain drop-in (oracle-matching) kernel on the same views, one launch per view
+    def plain_step():
+        for (cam, w, h), off in zip(cams, offs):
+            scene.render(cam, w, h, rgb[3 * off:3 * (off + w * h)])
+
+    plain_ms = None
+    if not precision:
+        for _ in range(max(1, args.warmup // 2)):
+            plain_step()
+        pm = timed_loop(plain_step, max(2, args.steps // 2))
+        plain_ms = sum(pm) / len(pm)
+
+    # counters of the oracle-matching kernel -> algorithmic bytes per step
+    tr_all = []
+    for (cam, w, h), off in zip(cams, offs):
+        if not (forms & F.FORM_EXACT):
+            break
+        tr = torch.zeros(w * h * 48, dtype=torch.uint8, device=dev)
+        tmp = torch.zeros(w * h * 3, device=dev)
+        scene.render_trace(cam, w, h, tmp, None, None, tr)
+        torch.cuda.synchronize(dev)
+        tr_all.append(np.frombuffer(tr.cpu().numpy().tobytes(), dtype=np.dtype(pkg.capi.TRACE_DTYPE)))
+    tr_cat = np.concatenate(tr_all)
+    b_test, b_blend = (32, 96 + 2) if precision else (48, 192 + 4)
+    alg_bytes = algorithmic_bytes(tr_cat, b_test, b_blend, 12)
+    peak, peak_kind = hbm_peak()
+    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    traffic = load_traffic().get(f"{args.config}:{'packed' if precision else 'fp32'}")
+    counters = {k: float(tr_cat[k].mean()) for k in ("n_inner", "n_leaf", "n_cand", "n_hit", "n_blend",
+                                                     "n_restart")}
+    out = {
+        "metric": METRIC if args.config == "scale" else f"Mrays/s ({args.config})",
+        "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16/fp16 storage, fp32 arithmetic" if precision else "f32", "data": "synthetic",
+        "config": {**desc, "form": "batched persistent kernel, CUDA graph", "autotuned": cfg.as_dict(),
+                   "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in e2e.items()},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                     else "fallback 6.8 TB/s",
+                     "algorithmic_bytes_per_step": alg_bytes, "bytes_per_ray": round(alg_bytes / rays, 1)},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "forms": {"plain_ms_per_step": plain_ms,
+                  "plain_mrays_s": round(rays / (plain_ms * 1e-3) / 1e6, 3) if plain_ms else None,
+                  "batched_over_plain": round(plain_ms / ms_step, 3) if plain_ms else None},
+        "counters_per_ray": counters,
+        "tree": {"nodes": tree.n_nodes, "ids": int(tree.offsets.size), "depth": tree.depth,
+                 "build_s": round(build_s, 2)},
+        "wall_s_timed": round(wall, 3),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(tree, rec, cams, args.cpu_seconds)
+    batch.close()
+    scene.close()
+    return out
+
+
+# ------------------------------------------------------------------ CPU arm
+def cpu_sample(tree, rec, cams, seconds: float, threads: int = 0):
+    """Render a strided ray sample of every view with the oracle (CPU), sized
+    to about `seconds` of work.  Returns (Mrays/s, rays, stride, threads)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    S = O.OracleScene(tree.nodes, tree.offsets, tree.aabb, O.invert_scales(rec))
+    nthr = threads or os.cpu_count() or 1
+
+    def run(stride):
+        n = 0
+        t = time.time()
+        for cam, w, h in cams:
+            pix = np.arange(0, w * h, stride, dtype=np.uint32)
+            O.render(S, cam, w, h, pixels=pix, threads=nthr)
+            n += pix.size
+        return n, time.time() - t
+
+    total = sum(w * h for _, w, h in cams)
+    stride = max(1, total // 20000)
+    n, dt = run(stride)
+    rate = n / max(dt, 1e-6)
+    stride = max(1, int(total / max(rate * seconds, 1)))
+    n, dt = run(stride)
+    return n / dt / 1e6, n, stride, nthr, dt
+
+
+def cpu_baseline(tree, rec, cams, seconds):
+    mr, n, stride, nthr, dt = cpu_sample(tree, rec, cams, seconds)
+    return {"value": round(mr, 4), "unit": UNIT, "cores": nthr, "kind": "port",
+            "sample": f"every {stride}th ray of each view ({n} rays, {dt:.1f}s), oracle FP32 transcription "
+                      f"of cudaRenderer.cu with OpenMP over rays"}
+
+
+def run_reference(args):
+    pkg = importlib.import_module("3dgrt_kdtree_gb300")
+    rec, cams, desc = make_workload(pkg, args.config)
+    tree = pkg.kdtree.build(rec)
+    per_step = max(2.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    res = []
+    for i in range(args.warmup + args.steps):
+        mr, n, stride, nthr, dt = cpu_sample(tree, rec, cams, per_step)
+        if i >= args.warmup:
+            res.append((mr, n, stride, dt))
+    value = statistics.mean(r[0] for r in res)
+    out = {
+        "metric": METRIC if args.config == "scale" else f"Mrays/s ({args.config})", "impl": "reference",
+        "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * statistics.mean(r[3] for r in res), 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {**desc, "form": "CPU transcription of the reference render kernel (oracle, OpenMP)"},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nthr, "kind": "port",
+                         "sample": f"every {res[-1][2]}th ray per view, {res[-1][1]} rays per step"},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", default="scale", choices=["scale", "small", "mid", "batching", "precision"])
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: default kernel config, no L2-flush buffer, no e2e/plain/CPU legs")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("[bench] warmup raised to 3")
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

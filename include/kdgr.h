@@ -181,12 +181,13 @@ typedef struct {
 } kdgr_view;
 
 typedef struct {
-  int32_t kbuf;          /* hit-buffer entries: 8 or 16 */
+  int32_t kbuf;          /* hit-buffer entries: 8 */
   int32_t stack;         /* short-stack entries: 16 or 24 */
   int32_t blocks_per_sm; /* persistent CTAs per SM; 0 = occupancy maximum */
-  int32_t chunk;         /* tiles a warp takes per queue operation (1..64) */
+  int32_t chunk;         /* work items taken per queue operation (1..64) */
   int32_t stage_top;     /* 1: stage the top tree levels in shared memory */
   int32_t precision;     /* 0: FP32 arrays (KDGR_FORM_FAST); 1: BF16/FP16 arrays (KDGR_FORM_PACKED) */
+  int32_t cta_tiles;     /* 0: each warp takes 8x4-pixel tiles; 1: each CTA takes 16x8 blocks */
 } kdgr_batch_config;
 
 void kdgr_batch_config_default(kdgr_batch_config* cfg);
