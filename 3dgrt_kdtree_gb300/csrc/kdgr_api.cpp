@@ -288,13 +288,13 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
       return fail("kdgr_scene_create: upload (tree)");
   }
   if (forms & KDGR_FORM_FAST) {
-    std::vector<float> tf(12 * (size_t)n, 0.f), op(n);
+    // rows of M = diag(1/s) R^T and b = M mu, in FP64, stored FP32
+    std::vector<float> tf(12 * (size_t)n), op(n);
     for (size_t i = 0; i < n; ++i) {
       const float* r = g + 64 * i;
       double m[3][3];
       quat_rt_d(r + 8, m);
       float* t = tf.data() + 12 * i;
-      op[i] = r[3];
       for (int row = 0; row < 3; ++row) {
         const double sc = giscl[3 * i + row];
         double b = 0;
@@ -305,6 +305,7 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
         }
         t[4 * row + 3] = (float)b;
       }
+      op[i] = r[3];
     }
     s->d_test_fast = A.alloc<float4>(3 * (size_t)n);
     s->d_opacity = A.alloc<float>(n);

@@ -19,8 +19,7 @@ struct kdgr_batch_s {
   ViewDesc* d_views = nullptr;
   uint32_t* d_queue = nullptr;
   int n_views = 0;
-  uint32_t total_tiles = 0;
-  uint32_t total_blocks = 0;
+  uint32_t totals[3] = {0, 0, 0};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -41,8 +40,8 @@ int batch_args(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb, 
 }
 
 // Stream-ordered scratch for one launch: view table + queue counter.
-int run_once(kdgr_scene_t s, const kdgr_batch_config& c, const std::vector<ViewDesc>& table, uint32_t tiles,
-             uint32_t blocks, float* rgb, float* alpha, float* depth, cudaStream_t st, const char* who) {
+int run_once(kdgr_scene_t s, const kdgr_batch_config& c, const std::vector<ViewDesc>& table,
+             const uint32_t totals[3], float* rgb, float* alpha, float* depth, cudaStream_t st, const char* who) {
   const size_t vbytes = table.size() * sizeof(ViewDesc);
   void* scratch = nullptr;
   cudaError_t e = cudaMallocAsync(&scratch, vbytes + 256, st);
@@ -52,7 +51,7 @@ int run_once(kdgr_scene_t s, const kdgr_batch_config& c, const std::vector<ViewD
   e = cudaMemcpyAsync(d_views, table.data(), vbytes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, 4, st);
   if (e == cudaSuccess)
-    e = launch_batch(s, c, d_views, (int)table.size(), tiles, blocks, rgb, alpha, depth, d_queue, st);
+    e = launch_batch(s, c, d_views, (int)table.size(), totals, rgb, alpha, depth, d_queue, st);
   const cudaError_t ef = cudaFreeAsync(scratch, st);
   if (e == cudaSuccess) e = ef;
   if (e != cudaSuccess) return cuda_fail(e, who);
@@ -65,13 +64,11 @@ extern "C" {
 
 void kdgr_batch_config_default(kdgr_batch_config* c) {
   if (!c) return;
-  c->kbuf = 8;
-  c->stack = 16;
+  c->schedule = KDGR_SCHED_CTA_BLOCKS;
+  c->min_blocks = 0;
   c->blocks_per_sm = 0;
   c->chunk = 1;
-  c->stage_top = 0;
   c->precision = 0;
-  c->cta_tiles = 1;
 }
 
 int kdgr_render_batch(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb, float* alpha, float* depth,
@@ -80,8 +77,8 @@ int kdgr_render_batch(kdgr_scene_t s, const kdgr_view* views, int n_views, float
   int rc = batch_args(s, views, n_views, rgb, cfg, c, "kdgr_render_batch");
   if (rc != KDGR_OK) return rc;
   std::vector<ViewDesc> table;
-  uint32_t tiles = 0, blocks = 0;
-  rc = make_view_table(views, n_views, table, &tiles, &blocks);
+  uint32_t totals[3] = {0, 0, 0};
+  rc = make_view_table(views, n_views, table, totals);
   if (rc != KDGR_OK) return rc;
   const cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -90,7 +87,7 @@ int kdgr_render_batch(kdgr_scene_t s, const kdgr_view* views, int n_views, float
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
   }
-  rc = run_once(s, c, table, tiles, blocks, rgb, alpha, depth, st, "kdgr_render_batch");
+  rc = run_once(s, c, table, totals, rgb, alpha, depth, st, "kdgr_render_batch");
   if (ms_out) {
     cudaEventRecord(e1, st);
     const cudaError_t e = cudaEventSynchronize(e1);
@@ -132,15 +129,14 @@ int kdgr_batch_create(kdgr_scene_t s, const kdgr_view* views, int n_views, float
   int rc = batch_args(s, views, n_views, rgb, cfg, c, "kdgr_batch_create");
   if (rc != KDGR_OK) return rc;
   std::vector<ViewDesc> table;
-  uint32_t tiles = 0, blocks = 0;
-  rc = make_view_table(views, n_views, table, &tiles, &blocks);
+  uint32_t totals[3] = {0, 0, 0};
+  rc = make_view_table(views, n_views, table, totals);
   if (rc != KDGR_OK) return rc;
   kdgr_batch_s* b = new kdgr_batch_s;
   b->scene = s;
   b->cfg = c;
   b->n_views = n_views;
-  b->total_tiles = tiles;
-  b->total_blocks = blocks;
+  for (int i = 0; i < 3; ++i) b->totals[i] = totals[i];
   cudaStream_t cap = nullptr;
   cudaError_t e = cudaMalloc(&b->d_views, table.size() * sizeof(ViewDesc));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, 4);
@@ -151,7 +147,7 @@ int kdgr_batch_create(kdgr_scene_t s, const kdgr_view* views, int n_views, float
   if (e == cudaSuccess) {
     cudaError_t le = cudaMemsetAsync(b->d_queue, 0, 4, cap);
     if (le == cudaSuccess)
-      le = launch_batch(s, c, b->d_views, n_views, tiles, blocks, rgb, alpha, depth, b->d_queue, cap);
+      le = launch_batch(s, c, b->d_views, n_views, totals, rgb, alpha, depth, b->d_queue, cap);
     e = cudaStreamEndCapture(cap, &b->graph);
     if (e == cudaSuccess) e = le;
   }
@@ -197,23 +193,20 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
   int rc = batch_args(s, views, n_views, rgb, &base, base, "kdgr_autotune");
   if (rc != KDGR_OK) return rc;
   std::vector<ViewDesc> table;
-  uint32_t tiles = 0, blocks = 0;
-  rc = make_view_table(views, n_views, table, &tiles, &blocks);
+  uint32_t totals[3] = {0, 0, 0};
+  rc = make_view_table(views, n_views, table, totals);
   if (rc != KDGR_OK) return rc;
   std::vector<kdgr_batch_config> cands;
-  for (int cta : {0, 1})
-    for (int stack : {16, 24})
-      for (int chunk : {1, 4})
-        for (int stage : {0, 1}) {
-          kdgr_batch_config c = base;
-          c.kbuf = 8;
-          c.cta_tiles = cta;
-          c.stack = stack;
-          c.chunk = chunk;
-          c.stage_top = stage;
-          c.blocks_per_sm = 0;
-          cands.push_back(c);
-        }
+  for (int minb : {0, 6, 8})
+    for (int sched : {KDGR_SCHED_WARP_TILES, KDGR_SCHED_CTA_BLOCKS})
+      for (int chunk : {1, 2}) {
+        kdgr_batch_config c = base;
+        c.min_blocks = minb;
+        c.schedule = sched;
+        c.chunk = chunk;
+        c.blocks_per_sm = 0;
+        cands.push_back(c);
+      }
   cudaStream_t st = nullptr;
   cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_autotune");
@@ -223,12 +216,12 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
   std::string rep;
   float best_ms = 1e30f;
   for (const kdgr_batch_config& c : cands) {
-    rc = run_once(s, c, table, tiles, blocks, rgb, nullptr, nullptr, st, "kdgr_autotune");  // warm-up
+    rc = run_once(s, c, table, totals, rgb, nullptr, nullptr, st, "kdgr_autotune");  // warm-up
     if (rc != KDGR_OK) break;
     std::vector<float> ts;
     for (int r = 0; r < 3 && rc == KDGR_OK; ++r) {
       cudaEventRecord(e0, st);
-      rc = run_once(s, c, table, tiles, blocks, rgb, nullptr, nullptr, st, "kdgr_autotune");
+      rc = run_once(s, c, table, totals, rgb, nullptr, nullptr, st, "kdgr_autotune");
       cudaEventRecord(e1, st);
       cudaEventSynchronize(e1);
       float ms = 0.f;
@@ -240,9 +233,8 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
     const float med = ts[ts.size() / 2];
     char line[256];
     snprintf(line, sizeof(line),
-             "{\"cta_tiles\": %d, \"stack\": %d, \"chunk\": %d, \"stage_top\": %d, \"precision\": %d, "
-             "\"ms\": %.4f}\n",
-             c.cta_tiles, c.stack, c.chunk, c.stage_top, c.precision, med);
+             "{\"schedule\": %d, \"min_blocks\": %d, \"chunk\": %d, \"precision\": %d, \"ms\": %.4f}\n",
+             c.schedule, c.min_blocks, c.chunk, c.precision, med);
     rep += line;
     if (med < best_ms) {
       best_ms = med;

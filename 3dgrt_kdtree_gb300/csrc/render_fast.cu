@@ -4,10 +4,10 @@
 // Same algorithm as the plain kernel (render_exact.cu): short-stack kd-tree
 // traversal front to back, per-leaf max-response test, hits composited in t
 // order until the opacity threshold.  What changes, for throughput:
-//   * arithmetic: FMA, rsqrt, __expf; the ray-Gaussian test reads the
-//     precomputed rows of M = diag(1/s) R^T with b = M mu folded in
-//     (gro = M o - b, grdu = M d), so t* = -(grd . gro) / |grdu| needs no
-//     per-candidate quaternion expansion or reciprocal;
+//   * arithmetic: FMA, fast reciprocal, __expf; the ray-Gaussian test reads
+//     the precomputed rows of M = diag(1/s) R^T with b = M mu folded in
+//     (gro = M o - b, grdu = M d) and rejects on t* before evaluating the
+//     Mahalanobis distance;
 //   * hits are accepted with t* in the half-open interval [t_near, t_far),
 //     so a Gaussian straddling a split plane is composited in one leaf only;
 //   * the top levels of the tree (breadth-first, up to 2047 nodes) are
@@ -17,9 +17,9 @@
 //   * a leaf's candidates are fetched two at a time (both ID and record loads
 //     in flight before either test), doubling the memory-level parallelism
 //     of the latency-bound candidate loop;
-//   * work items are either 8x4 tiles taken per warp or 16x8 blocks taken per
-//     CTA (its four warps render neighbouring tiles and share L1); the
-//     autotuner picks one.
+//   * pixels are handed out in spatially coherent units (8x4 warp tiles or
+//     16x8 CTA blocks) so the rays sharing an SM's L1 are neighbours; the
+//     autotuner picks the schedule and the register cap (occupancy).
 //   * precision form: FP16 inverse scales / quaternion / opacity and BF16
 //     SH (32 + 96 bytes per Gaussian instead of 64 + 192); Gaussians whose
 //     scale ratio exceeds 1e3 read factors from the FP64 upload precompute.
@@ -48,8 +48,7 @@ constexpr int kWarps = 4;
 constexpr int kThreads = kWarps * 32;
 constexpr int kTileW = 8, kTileH = 4;     // pixels per warp tile
 constexpr int kBlockW = 16, kBlockH = 8;  // pixels per CTA block (4 warps of 8x4)
-constexpr int kHits = 8;                  // hit-buffer entries
-constexpr uint32_t kMaxTop = 2047;
+constexpr int kHits = 4;                  // hit-buffer entries per leaf pass (a leaf averages <1 hit)
 
 struct F3 {
   float x, y, z;
@@ -70,8 +69,13 @@ __device__ __forceinline__ float2 h2f(uint32_t w) {
 
 // ----------------------------------------------------------- candidate test
 // Records of one candidate as loaded from memory.
+//   FP32:   (M0, b0) (M1, b1) (M2, b2): rows of M = diag(1/s) R^T and
+//           b = M mu (FP64 upload precompute).  Storing Sigma^-1 = M^T M
+//           instead would square the condition number (a scale ratio of
+//           2500 gives ~6e6, beyond FP32), so the factor is kept;
+//   packed: a = (mu, +-opacity), b = FP16 halves (1/s, quaternion).
 struct Rec {
-  float4 a, b, c;  // FP32: (M0,b0)(M1,b1)(M2,b2).  Packed: a = (mu, +-opacity), b = halves
+  float4 a, b, c;
 };
 
 template <bool PACKED>
@@ -86,13 +90,11 @@ __device__ __forceinline__ Rec load_rec(const FastView& S, uint32_t gid) {
     const uint4 u0 = __ldg(S.packed + 2ull * gid), u1 = __ldg(S.packed + 2ull * gid + 1);
     r.a = make_float4(__uint_as_float(u0.x), __uint_as_float(u0.y), __uint_as_float(u0.z), __uint_as_float(u0.w));
     r.b = make_float4(__uint_as_float(u1.x), __uint_as_float(u1.y), __uint_as_float(u1.z), __uint_as_float(u1.w));
-    r.c = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   return r;
 }
 
-// t* and the squared Mahalanobis distance of the ray (cudaRenderer.cu:
-// 1115-1127) from the rows of M = diag(1/s) R^T:
+// The same test from the rows of M = diag(1/s) R^T (A = M^T M):
 // grdu = M d, t* = -(grdu . gro) / |grdu|^2, gray = |grdu x gro|^2 / |grdu|^2.
 __device__ __forceinline__ bool finish_test(F3 m0, F3 m1, F3 m2, F3 gro, F3 d, float t_near, float t_far,
                                             float* t_out, float* gray_out) {
@@ -206,12 +208,13 @@ __device__ __forceinline__ F3 eval_sh_fast(const FastView& S, uint32_t gid, F3 d
 
 // K smallest (t, leaf position) keys of a leaf pass, ascending; equal t keep
 // leaf order (the stable sortHits, cudaRenderer.cu:415-426).
+template <int K>
 struct HitBuf {
-  float t[kHits], g[kHits];
-  uint32_t i[kHits];
+  float t[K], g[K];
+  uint32_t i[K];
   __device__ __forceinline__ void clear() {
 #pragma unroll
-    for (int k = 0; k < kHits; ++k) {
+    for (int k = 0; k < K; ++k) {
       t[k] = __int_as_float(0x7f800000);
       g[k] = 0.f;
       i[k] = 0u;
@@ -221,7 +224,7 @@ struct HitBuf {
   __device__ __forceinline__ bool insert(float ct, float cg, uint32_t ci) {
     bool placed = false;
 #pragma unroll
-    for (int k = 0; k < kHits; ++k) {
+    for (int k = 0; k < K; ++k) {
       const bool sw = placed || (ct < t[k]);
       const float t0 = t[k], g0 = g[k];
       const uint32_t i0 = i[k];
@@ -238,178 +241,209 @@ struct HitBuf {
 };
 
 // ------------------------------------------------------------------ one ray
-template <int SD, bool PACKED, bool STAGE>
-__device__ __forceinline__ void trace_ray(const FastView& S, const uint2* s_top, uint32_t n_top,
-                                          uint32_t (*s_id)[kThreads], float (*s_t)[kThreads], int tid,
-                                          const CamInfo& C, int x, int y, uint32_t* status, float* acc_out) {
-  auto fetch = [&](uint32_t i) -> uint2 { return (STAGE && i < n_top) ? s_top[i] : __ldg(S.nodes + i); };
+constexpr int kStack = 16;  // short-stack ring entries (ring + root restart as the reference)
+
+// Per-lane ray state; one leaf is processed per call of leaf_step.
+struct Ray {
+  F3 o, d, inv;
+  float t_near, t_far, t_scene_far;
+  float r, g, b, A, D;
+  uint32_t cur, steps;
+  unsigned top, quant;
+};
+
+__device__ __forceinline__ float sel3(const F3& v, uint32_t axis) { return axis == 0 ? v.x : axis == 1 ? v.y : v.z; }
+
+// Ray generation (cudaRenderer.cu:2336-2339) and the scene-box slab test
+// (:379-399).  Returns false when the ray misses the box.
+__device__ __forceinline__ bool ray_init(const FastView& S, const CamInfo& C, int x, int y, Ray& R) {
   const float sx = (float)x + 0.5f, sy = (float)y + 0.5f;
-  const F3 o = mk(__ldg(&C.eye[0]), __ldg(&C.eye[1]), __ldg(&C.eye[2]));
+  R.o = mk(__ldg(&C.eye[0]), __ldg(&C.eye[1]), __ldg(&C.eye[2]));
+  const float sxx = sx * __ldg(&C.step_x), syy = sy * __ldg(&C.step_y);
   F3 d;
-  {
-    const float sxx = sx * __ldg(&C.step_x), syy = sy * __ldg(&C.step_y);
-    d.x = __ldg(&C.start[0]) + __ldg(&C.u[0]) * sxx - __ldg(&C.v[0]) * syy - o.x;
-    d.y = __ldg(&C.start[1]) + __ldg(&C.u[1]) * sxx - __ldg(&C.v[1]) * syy - o.y;
-    d.z = __ldg(&C.start[2]) + __ldg(&C.u[2]) * sxx - __ldg(&C.v[2]) * syy - o.z;
-    const float il = rsqrtf(dot3(d, d));
-    d.x *= il;
-    d.y *= il;
-    d.z *= il;
-  }
-  const float inv[3] = {1.f / d.x, 1.f / d.y, 1.f / d.z};
-  const float oo[3] = {o.x, o.y, o.z};
-  float acc_r = 0.f, acc_g = 0.f, acc_b = 0.f, A = 0.f, D = 0.f;
+  d.x = __ldg(&C.start[0]) + __ldg(&C.u[0]) * sxx - __ldg(&C.v[0]) * syy - R.o.x;
+  d.y = __ldg(&C.start[1]) + __ldg(&C.u[1]) * sxx - __ldg(&C.v[1]) * syy - R.o.y;
+  d.z = __ldg(&C.start[2]) + __ldg(&C.u[2]) * sxx - __ldg(&C.v[2]) * syy - R.o.z;
+  const float il = rsqrtf(dot3(d, d));
+  R.d = mk(d.x * il, d.y * il, d.z * il);
+  R.inv = mk(1.f / R.d.x, 1.f / R.d.y, 1.f / R.d.z);
+  R.r = R.g = R.b = R.A = R.D = 0.f;
   float tmin = 1e-2f, tmax = FLT_MAX;
+  const float oo[3] = {R.o.x, R.o.y, R.o.z}, iv[3] = {R.inv.x, R.inv.y, R.inv.z};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const float l1 = (S.bmin[a] - oo[a]) * inv[a];
-    const float l2 = (S.bmax[a] - oo[a]) * inv[a];
+    const float l1 = (S.bmin[a] - oo[a]) * iv[a];
+    const float l2 = (S.bmax[a] - oo[a]) * iv[a];
     tmin = fmaxf(fminf(l1, l2), tmin);
     tmax = fminf(fmaxf(l1, l2), tmax);
   }
-  if ((tmax >= tmin) & (tmax >= 0.f)) {
-    const float t_scene_far = tmax;
-    float t_near = tmin, t_far = tmax;
-    uint32_t cur = 0, steps = 0;
-    unsigned top = SD - 1, quant = 0;
-    while (A < 0.99f) {
-      uint2 nd = fetch(cur);
-      if (++steps > kMaxRaySteps) {
-        atomicOr(status, kStatusStepLimit);
-        break;
-      }
-      bool bad = false;
-      while ((nd.x & 7u) != 3u) {
-        const uint32_t child = nd.x >> 3;
-        const uint32_t axis = nd.x & 3u;
-        const float o_a = axis == 0 ? oo[0] : axis == 1 ? oo[1] : oo[2];
-        const float i_a = axis == 0 ? inv[0] : axis == 1 ? inv[1] : inv[2];
-        const float t_split = (__uint_as_float(nd.y) - o_a) * i_a;
-        const unsigned sign = __float_as_uint(i_a) >> 31;
-        const uint32_t idx = child + (sign ^ (t_split <= t_near ? 1u : 0u));
-        if (t_near < t_split && t_split < t_far) {
-          if (++top == SD) top = 0;
-          quant = min(quant + 1, (unsigned)SD);
-          s_id[top][tid] = child + (sign ^ 1u);
-          s_t[top][tid] = t_far;
-          t_far = t_split;
-        }
-        if (child + 1 >= S.n_nodes || ++steps > kMaxRaySteps) {
-          atomicOr(status, child + 1 >= S.n_nodes ? kStatusBadNode : kStatusStepLimit);
-          bad = true;
-          break;
-        }
-        cur = idx;
-        nd = fetch(cur);
-      }
-      if (bad) break;
-      const uint32_t cnt = nd.x >> 3, base = nd.y;
-      if ((uint64_t)base + cnt > S.n_offsets) {
-        atomicOr(status, kStatusBadLeaf);
-        break;
-      }
-      bool have_last = false, saturated = false;
-      float last_t = 0.f;
-      uint32_t last_i = 0;
-      while (true) {
-        HitBuf hb;
-        hb.clear();
-        bool overflow = false;
-        for (uint32_t i = 0; i < cnt; i += 2) {
-          const bool two = i + 1 < cnt;
-          const uint32_t g0 = __ldg(S.offsets + base + i);
-          const uint32_t g1 = two ? __ldg(S.offsets + base + i + 1) : g0;
-          if (g0 >= S.n_gauss || g1 >= S.n_gauss) {
-            atomicOr(status, kStatusBadId);
-            bad = true;
-            break;
-          }
-          const Rec r0 = load_rec<PACKED>(S, g0);
-          const Rec r1 = load_rec<PACKED>(S, g1);
-          float t, g;
-          if (test_rec<PACKED>(S, g0, r0, o, d, t_near, t_far, &t, &g) &&
-              (!have_last || t > last_t || (t == last_t && i > last_i)))
-            overflow |= hb.insert(t, g, i);
-          if (two && test_rec<PACKED>(S, g1, r1, o, d, t_near, t_far, &t, &g) &&
-              (!have_last || t > last_t || (t == last_t && i + 1 > last_i)))
-            overflow |= hb.insert(t, g, i + 1);
-        }
-        if (bad) break;
-#pragma unroll
-        for (int k = 0; k < kHits; ++k) {
-          if (hb.t[k] == __int_as_float(0x7f800000)) break;
-          const uint32_t gid = __ldg(S.offsets + base + hb.i[k]);
-          const float gres = __expf(-0.0555555555556f * hb.g[k] * hb.g[k]);
-          const float alpha = fminf(0.99f, gauss_opacity<PACKED>(S, gid) * gres);
-          if (gres < 0.0113f || alpha < 1.0f / 255.0f) continue;
-          const F3 c = eval_sh_fast<PACKED>(S, gid, d);
-          const float w = alpha * (1.f - A);
-          acc_r = fmaf(c.x, w, acc_r);
-          acc_g = fmaf(c.y, w, acc_g);
-          acc_b = fmaf(c.z, w, acc_b);
-          D = fmaf(hb.t[k], w, D);
-          A += w;
-          if (A > 0.99f) {
-            saturated = true;
-            break;
-          }
-        }
-        if (saturated || !overflow) break;
-        have_last = true;
-        last_t = hb.t[kHits - 1];
-        last_i = hb.i[kHits - 1];
-      }
-      if (bad) break;
-      if ((A > 0.99f) | (t_far >= t_scene_far)) break;
-      if (quant == 0) {
-        cur = 0;
-        t_near = t_far;
-        t_far = t_scene_far;
-      } else {
-        const uint32_t id = s_id[top][tid];
-        const float tm = s_t[top][tid];
-        if (top == 0) top = SD;
-        --top;
-        --quant;
-        cur = id;
-        t_near = t_far;
-        t_far = tm;
-      }
-    }
-  }
-  acc_out[0] = acc_r;
-  acc_out[1] = acc_g;
-  acc_out[2] = acc_b;
-  acc_out[3] = A;
-  acc_out[4] = D;
+  R.t_near = tmin;
+  R.t_far = tmax;
+  R.t_scene_far = tmax;
+  R.cur = 0;
+  R.steps = 0;
+  R.top = kStack - 1;
+  R.quant = 0;
+  return (tmax >= tmin) & (tmax >= 0.f);
 }
 
-template <int SD, bool PACKED, bool STAGE, bool CTA>
-__global__ void __launch_bounds__(kThreads) k_render_batch(FastView S, const ViewDesc* __restrict__ views, int n_views,
-                                                           uint32_t total_items, float* __restrict__ rgb,
-                                                           float* __restrict__ alpha_out,
-                                                           float* __restrict__ depth_out, uint32_t* queue,
-                                                           uint32_t* status, int chunk) {
-  __shared__ uint2 s_top[STAGE ? kMaxTop : 1];
-  __shared__ uint32_t s_id[SD][kThreads];
-  __shared__ float s_t[SD][kThreads];
+// Descend from R.cur to the next leaf, test and composite it, then pop or
+// restart (singlePassIntersectGaussian_sortNode_onlyShortStack,
+// cudaRenderer.cu:1552-1708).  Returns true when the ray is finished.
+template <int K, bool PACKED>
+__device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kThreads], float (*s_t)[kThreads],
+                                          int tid, Ray& R, uint32_t* status) {
+  uint2 nd = __ldg(S.nodes + R.cur);
+  if (++R.steps > kMaxRaySteps) {
+    atomicOr(status, kStatusStepLimit);
+    return true;
+  }
+  while ((nd.x & 7u) != 3u) {
+    const uint32_t child = nd.x >> 3;
+    const uint32_t axis = nd.x & 3u;
+    const float i_a = sel3(R.inv, axis);
+    const float t_split = (__uint_as_float(nd.y) - sel3(R.o, axis)) * i_a;
+    const unsigned sign = __float_as_uint(i_a) >> 31;
+    const uint32_t idx = child + (sign ^ (t_split <= R.t_near ? 1u : 0u));
+    if (R.t_near < t_split && t_split < R.t_far) {
+      if (++R.top == kStack) R.top = 0;
+      R.quant = min(R.quant + 1, (unsigned)kStack);
+      s_id[R.top][tid] = child + (sign ^ 1u);
+      s_t[R.top][tid] = R.t_far;
+      R.t_far = t_split;
+    }
+    if (child + 1 >= S.n_nodes || ++R.steps > kMaxRaySteps) {
+      atomicOr(status, child + 1 >= S.n_nodes ? kStatusBadNode : kStatusStepLimit);
+      return true;
+    }
+    R.cur = idx;
+    nd = __ldg(S.nodes + R.cur);
+  }
+  const uint32_t cnt = nd.x >> 3, base = nd.y;
+  if ((uint64_t)base + cnt > S.n_offsets) {
+    atomicOr(status, kStatusBadLeaf);
+    return true;
+  }
+  bool have_last = false;
+  float last_t = 0.f;
+  uint32_t last_i = 0;
+  while (true) {
+    HitBuf<K> hb;
+    hb.clear();
+    bool overflow = false;
+    for (uint32_t i = 0; i < cnt; i += 2) {
+      const bool two = i + 1 < cnt;
+      const uint32_t g0 = __ldg(S.offsets + base + i);
+      const uint32_t g1 = two ? __ldg(S.offsets + base + i + 1) : g0;
+      if (g0 >= S.n_gauss || g1 >= S.n_gauss) {
+        atomicOr(status, kStatusBadId);
+        return true;
+      }
+      const Rec r0 = load_rec<PACKED>(S, g0);
+      const Rec r1 = load_rec<PACKED>(S, g1);
+      float t, g;
+      if (test_rec<PACKED>(S, g0, r0, R.o, R.d, R.t_near, R.t_far, &t, &g) &&
+          (!have_last || t > last_t || (t == last_t && i > last_i)))
+        overflow |= hb.insert(t, g, i);
+      if (two && test_rec<PACKED>(S, g1, r1, R.o, R.d, R.t_near, R.t_far, &t, &g) &&
+          (!have_last || t > last_t || (t == last_t && i + 1 > last_i)))
+        overflow |= hb.insert(t, g, i + 1);
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (hb.t[k] == __int_as_float(0x7f800000)) break;
+      const uint32_t gid = __ldg(S.offsets + base + hb.i[k]);
+      const float gres = __expf(-0.0555555555556f * hb.g[k] * hb.g[k]);
+      const float alpha = fminf(0.99f, gauss_opacity<PACKED>(S, gid) * gres);
+      if (gres < 0.0113f || alpha < 1.0f / 255.0f) continue;
+      const F3 c = eval_sh_fast<PACKED>(S, gid, R.d);
+      const float w = alpha * (1.f - R.A);
+      R.r = fmaf(c.x, w, R.r);
+      R.g = fmaf(c.y, w, R.g);
+      R.b = fmaf(c.z, w, R.b);
+      R.D = fmaf(hb.t[k], w, R.D);
+      R.A += w;
+      if (R.A > 0.99f) return true;
+    }
+    if (!overflow) break;
+    have_last = true;
+    last_t = hb.t[K - 1];
+    last_i = hb.i[K - 1];
+  }
+  if (R.t_far >= R.t_scene_far) return true;
+  if (R.quant == 0) {
+    R.cur = 0;
+    R.t_near = R.t_far;
+    R.t_far = R.t_scene_far;
+  } else {
+    const uint32_t id = s_id[R.top][tid];
+    const float tm = s_t[R.top][tid];
+    if (R.top == 0) R.top = kStack;
+    --R.top;
+    --R.quant;
+    R.cur = id;
+    R.t_near = R.t_far;
+    R.t_far = tm;
+  }
+  return false;
+}
+
+__device__ __forceinline__ int find_view(const ViewDesc* views, int n_views, uint32_t item, int sched) {
+  int lo = 0, hi = n_views - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const uint32_t b = sched == KDGR_SCHED_WARP_TILES ? __ldg(&views[mid].wt_base) : __ldg(&views[mid].cb_base);
+    if (b <= item) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Render the ray of pixel (x, y) of view V to completion and store it.
+template <int K, bool PACKED>
+__device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, int x, int y,
+                                          uint32_t (*s_id)[kThreads], float (*s_t)[kThreads], int tid, float* rgb,
+                                          float* alpha_out, float* depth_out, uint32_t* status) {
+  const int W = __ldg(&V.W), H = __ldg(&V.H);
+  if (x >= W || y >= H) return;
+  Ray R;
+  if (ray_init(S, V.cam, x, y, R)) {
+    while (R.A < 0.99f && !leaf_step<K, PACKED>(S, s_id, s_t, tid, R, status)) {
+    }
+  }
+  const size_t idx = (size_t)__ldg(&V.out_off) + (size_t)(H - 1 - y) * W + x;  // rows flipped per view
+  rgb[3 * idx] = R.r;
+  rgb[3 * idx + 1] = R.g;
+  rgb[3 * idx + 2] = R.b;
+  if (alpha_out) alpha_out[idx] = R.A;
+  if (depth_out) depth_out[idx] = R.D;
+}
+
+// Persistent kernel.  Schedules (include/kdgr.h):
+//   WARP_TILES: each warp takes `chunk` 8x4 tiles from the global queue;
+//   CTA_BLOCKS: each CTA takes `chunk` 16x8 blocks (barrier per block) and
+//               its four warps render the four quarters, so the rays sharing
+//               the SM's L1 are neighbours.
+// MINB caps registers so that MINB CTAs fit per SM (0: compiler's choice).
+template <bool PACKED, int SCHED, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, const ViewDesc* __restrict__ views,
+                                                                 int n_views, uint32_t total_items,
+                                                                 float* __restrict__ rgb,
+                                                                 float* __restrict__ alpha_out,
+                                                                 float* __restrict__ depth_out, uint32_t* queue,
+                                                                 uint32_t* status, int chunk) {
+  __shared__ uint32_t s_id[kStack][kThreads];
+  __shared__ float s_t[kStack][kThreads];
   __shared__ uint32_t s_work;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t n_top = STAGE ? min(S.top_nodes, kMaxTop) : 0u;
-  if constexpr (STAGE) {
-    for (uint32_t i = tid; i < n_top; i += kThreads) s_top[i] = __ldg(S.nodes + i);
-    __syncthreads();
-  }
   while (true) {
     uint32_t first;
-    if constexpr (CTA) {
-      // the CTA takes `chunk` 16x8 blocks; its warps render the four quarters
+    if constexpr (SCHED == KDGR_SCHED_CTA_BLOCKS) {
       __syncthreads();
       if (tid == 0) s_work = atomicAdd(queue, (uint32_t)chunk);
       __syncthreads();
       first = s_work;
     } else {
-      // each warp takes `chunk` 8x4 tiles
       uint32_t f = 0;
       if (lane == 0) f = atomicAdd(queue, (uint32_t)chunk);
       first = __shfl_sync(0xFFFFFFFFu, f, 0);
@@ -417,16 +451,9 @@ __global__ void __launch_bounds__(kThreads) k_render_batch(FastView S, const Vie
     if (first >= total_items) break;
     const uint32_t last = min(first + (uint32_t)chunk, total_items);
     for (uint32_t item = first; item < last; ++item) {
-      int lo = 0, hi = n_views - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        const uint32_t b = CTA ? __ldg(&views[mid].cb_base) : __ldg(&views[mid].wt_base);
-        if (b <= item) lo = mid;
-        else hi = mid - 1;
-      }
-      const ViewDesc& V = views[lo];
+      const ViewDesc& V = views[find_view(views, n_views, item, SCHED)];
       int x, y;
-      if (CTA) {
+      if (SCHED == KDGR_SCHED_CTA_BLOCKS) {
         const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
         x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
         y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
@@ -435,16 +462,7 @@ __global__ void __launch_bounds__(kThreads) k_render_batch(FastView S, const Vie
         x = (int)(lt % nx) * kTileW + (lane & 7);
         y = (int)(lt / nx) * kTileH + (lane >> 3);
       }
-      const int W = __ldg(&V.W), H = __ldg(&V.H);
-      if (x >= W || y >= H) continue;
-      float acc[5];
-      trace_ray<SD, PACKED, STAGE>(S, s_top, n_top, s_id, s_t, tid, V.cam, x, y, status, acc);
-      const size_t idx = (size_t)__ldg(&V.out_off) + (size_t)(H - 1 - y) * W + x;
-      rgb[3 * idx] = acc[0];
-      rgb[3 * idx + 1] = acc[1];
-      rgb[3 * idx + 2] = acc[2];
-      if (alpha_out) alpha_out[idx] = acc[3];
-      if (depth_out) depth_out[idx] = acc[4];
+      render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
     }
   }
 }
@@ -478,19 +496,21 @@ __global__ void k_aniso_fp64(const float* __restrict__ src, uint32_t n, float4* 
 using KernelFn = void (*)(FastView, const ViewDesc*, int, uint32_t, float*, float*, float*, uint32_t*, uint32_t*,
                           int);
 
-template <bool PACKED, bool STAGE, bool CTA>
-KernelFn pick_sd(int stack) {
-  return stack >= 24 ? k_render_batch<24, PACKED, STAGE, CTA> : k_render_batch<16, PACKED, STAGE, CTA>;
+template <bool PACKED, int SCHED>
+KernelFn pick_minb(int minb) {
+  if (minb >= 8) return k_render_batch<PACKED, SCHED, 8>;
+  if (minb >= 6) return k_render_batch<PACKED, SCHED, 6>;
+  return k_render_batch<PACKED, SCHED, 0>;
 }
 
-template <bool PACKED, bool STAGE>
-KernelFn pick_cta(const kdgr_batch_config& c) {
-  return c.cta_tiles ? pick_sd<PACKED, STAGE, true>(c.stack) : pick_sd<PACKED, STAGE, false>(c.stack);
+template <bool PACKED>
+KernelFn pick_sched(const kdgr_batch_config& c) {
+  return c.schedule == KDGR_SCHED_CTA_BLOCKS ? pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS>(c.min_blocks)
+                                             : pick_minb<PACKED, KDGR_SCHED_WARP_TILES>(c.min_blocks);
 }
 
 KernelFn pick_kernel(const kdgr_batch_config& c) {
-  if (c.precision) return c.stage_top ? pick_cta<true, true>(c) : pick_cta<true, false>(c);
-  return c.stage_top ? pick_cta<false, true>(c) : pick_cta<false, false>(c);
+  return c.precision ? pick_sched<true>(c) : pick_sched<false>(c);
 }
 
 int g_num_sms = 0;
@@ -508,8 +528,7 @@ int num_sms() {
 }  // namespace
 
 // Host: view table and total tile count for a list of views.
-int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t* total_tiles,
-                    uint32_t* total_blocks) {
+int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]) {
   out.resize(n_views);
   uint64_t wbase = 0, cbase = 0;
   for (int v = 0; v < n_views; ++v) {
@@ -534,8 +553,9 @@ int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& 
       return KDGR_ERR_LIMIT;
     }
   }
-  *total_tiles = (uint32_t)wbase;
-  *total_blocks = (uint32_t)cbase;
+  totals[0] = (uint32_t)wbase;
+  totals[1] = (uint32_t)cbase;
+  totals[2] = 0;
   return KDGR_OK;
 }
 
@@ -552,8 +572,12 @@ int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
     set_error("batch config: chunk must be in 1..64");
     return KDGR_ERR_INVALID_ARG;
   }
-  if (c.kbuf != kHits || (c.stack != 16 && c.stack != 24)) {
-    set_error("batch config: kbuf must be 8 and stack 16 or 24");
+  if (c.schedule != KDGR_SCHED_WARP_TILES && c.schedule != KDGR_SCHED_CTA_BLOCKS) {
+    set_error("batch config: unknown schedule");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (c.min_blocks != 0 && c.min_blocks != 6 && c.min_blocks != 8) {
+    set_error("batch config: min_blocks must be 0, 6 or 8");
     return KDGR_ERR_INVALID_ARG;
   }
   return KDGR_OK;
@@ -561,8 +585,9 @@ int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
 
 // Launch the persistent kernel.  `queue` must read 0 when the kernel starts.
 cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewDesc* d_views, int n_views,
-                         uint32_t total_tiles, uint32_t total_blocks, float* rgb, float* alpha, float* depth,
-                         uint32_t* queue, cudaStream_t st) {
+                         const uint32_t totals[3], float* rgb, float* alpha, float* depth, uint32_t* queue,
+                         cudaStream_t st) {
+  const uint32_t total_tiles = totals[0], total_blocks = totals[1];
   KernelFn fn = pick_kernel(c);
   int per_sm = c.blocks_per_sm;
   if (per_sm <= 0) {
@@ -571,13 +596,14 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
     if (e != cudaSuccess) return e;
     per_sm = occ > 0 ? occ : 1;
   }
-  const uint32_t total = c.cta_tiles ? total_blocks : total_tiles;
+  const uint32_t total = c.schedule == KDGR_SCHED_WARP_TILES ? total_tiles : total_blocks;
+  const int chunk = c.chunk;
   uint64_t blocks = (uint64_t)num_sms() * per_sm;
-  const uint64_t grabs = ((uint64_t)total + c.chunk - 1) / c.chunk;
-  const uint64_t cap = c.cta_tiles ? grabs : (grabs + kWarps - 1) / kWarps;
+  const uint64_t grabs = ((uint64_t)total + chunk - 1) / chunk;
+  const uint64_t cap = c.schedule == KDGR_SCHED_WARP_TILES ? (grabs + kWarps - 1) / kWarps : grabs;
   if (blocks > cap) blocks = cap > 0 ? cap : 1;
   fn<<<(unsigned)blocks, kThreads, 0, st>>>(s->fast_view(), d_views, n_views, total, rgb, alpha, depth, queue,
-                                            s->d_status, c.chunk);
+                                            s->d_status, chunk);
   return cudaGetLastError();
 }
 

@@ -71,12 +71,12 @@ void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std:
 // opacity, and the FP64 upload-time factors of anisotropic Gaussians.
 int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh, DevAlloc& A);
 // Batched rendering (render_fast.cu).
-int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t* total_tiles,
-                    uint32_t* total_blocks);
+// totals: 8x4 tiles, 16x8 blocks and 32x16 super-blocks over all views.
+int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]);
 int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c);
 cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewDesc* d_views, int n_views,
-                         uint32_t total_tiles, uint32_t total_blocks, float* rgb, float* alpha, float* depth,
-                         uint32_t* queue, cudaStream_t st);
+                         const uint32_t totals[3], float* rgb, float* alpha, float* depth, uint32_t* queue,
+                         cudaStream_t st);
 int batch_sms();
 // Scale ratio above which a Gaussian's factors come from the FP64 precompute.
 constexpr double kAnisoRatio = 1e3;

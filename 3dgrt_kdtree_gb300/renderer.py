@@ -24,6 +24,7 @@ from . import capi
 from .kdtree import KdTree
 
 FORM_EXACT, FORM_FAST, FORM_PACKED = 0x10, 0x20, 0x40
+SCHED_WARP_TILES, SCHED_CTA_BLOCKS = 0, 1
 SCALES_INVERTED = 0x1
 
 
@@ -40,9 +41,8 @@ class View(ctypes.Structure):
 
 
 class BatchConfig(ctypes.Structure):
-    _fields_ = [("kbuf", ctypes.c_int32), ("stack", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("chunk", ctypes.c_int32), ("stage_top", ctypes.c_int32), ("precision", ctypes.c_int32),
-                ("cta_tiles", ctypes.c_int32)]
+    _fields_ = [("schedule", ctypes.c_int32), ("min_blocks", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
+                ("chunk", ctypes.c_int32), ("precision", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

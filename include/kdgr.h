@@ -180,14 +180,16 @@ typedef struct {
   uint64_t out_offset; /* first pixel of this view in the output buffers */
 } kdgr_view;
 
+/* How the persistent kernel hands out pixels. */
+#define KDGR_SCHED_WARP_TILES 0  /* each warp takes 8x4-pixel tiles */
+#define KDGR_SCHED_CTA_BLOCKS 1  /* each CTA takes 16x8 blocks; its 4 warps render the quarters */
+
 typedef struct {
-  int32_t kbuf;          /* hit-buffer entries: 8 */
-  int32_t stack;         /* short-stack entries: 16 or 24 */
+  int32_t schedule;      /* KDGR_SCHED_* */
+  int32_t min_blocks;    /* register cap: 0 (compiler), 6 or 8 resident 128-thread CTAs per SM */
   int32_t blocks_per_sm; /* persistent CTAs per SM; 0 = occupancy maximum */
   int32_t chunk;         /* work items taken per queue operation (1..64) */
-  int32_t stage_top;     /* 1: stage the top tree levels in shared memory */
   int32_t precision;     /* 0: FP32 arrays (KDGR_FORM_FAST); 1: BF16/FP16 arrays (KDGR_FORM_PACKED) */
-  int32_t cta_tiles;     /* 0: each warp takes 8x4-pixel tiles; 1: each CTA takes 16x8 blocks */
 } kdgr_batch_config;
 
 void kdgr_batch_config_default(kdgr_batch_config* cfg);
@@ -213,9 +215,10 @@ int kdgr_batch_run(kdgr_batch_t batch, void* stream);
 int kdgr_batch_destroy(kdgr_batch_t batch);
 
 /* Time the kernel variants on the given views and return the fastest
- * configuration (tile work per queue operation, hit-buffer and stack sizes,
- * CTAs per SM, shared-memory staging).  d_rgb must hold the views' pixels.
- * report (may be null) receives a JSON line per variant. */
+ * configuration (pixel schedule, register cap, work items per queue
+ * operation).
+ * d_rgb must hold the views' pixels.  report (may be null) receives a JSON
+ * line per variant. */
 int kdgr_autotune(kdgr_scene_t scene, const kdgr_view* views, int n_views, int precision, float* d_rgb,
                   kdgr_batch_config* best, char* report, int report_len);
 

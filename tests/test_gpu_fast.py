@@ -90,8 +90,8 @@ def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
     views, total, _ = F.make_views(cams)
     rgb = torch.zeros(total * 3, device=cuda)
     best, report = scene.autotune(views, len(cams), rgb)
-    assert best.kbuf == 8 and best.stack in (16, 24) and best.chunk in (1, 4) and best.cta_tiles in (0, 1)
-    assert len(report.strip().splitlines()) == 16
+    assert best.schedule in (0, 1) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
+    assert len(report.strip().splitlines()) == 12
     ref = torch.zeros_like(rgb)
     scene.render_batch(views, len(cams), ref)
     out = torch.zeros_like(rgb)
