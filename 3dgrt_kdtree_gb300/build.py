@@ -29,7 +29,7 @@ CU_UNITS = {
     "render_exact.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "render_fast.cu": [],
 }
-CPP_UNITS = ["kdbuild.cpp", "kdgr_tree_api.cpp", "kdgr_api.cpp", "kdgr_batch_api.cpp"]
+CPP_UNITS = ["kdbuild.cpp", "kdgr_tree_api.cpp", "kdgr_api.cpp", "kdgr_batch_api.cpp", "kdgr_reference_api.cpp"]
 
 
 def _cuda_home() -> str:

@@ -1,0 +1,144 @@
+// kdgr_reference_api.cpp -- the reference's C++ render entry points
+// (include/kdgr_reference_api.h) over the C ABI.  One global scene and the
+// last frame's parameters, as the reference keeps global device state
+// (cudaRenderer.cu:314-360).
+#include "kdgr_reference_api.h"
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "kdgr.h"
+
+namespace {
+
+std::mutex g_mu;
+kdgr_scene_t g_scene = nullptr;
+kdgr_tree g_tree;  // arrays handed out by read_kd_tree_from_file
+bool g_have_tree = false;
+bool g_have_frame = false;
+kdgr_camera g_last_cam;
+int g_last_w = 0, g_last_h = 0;
+
+kdgr_camera to_camera(const Camera& c) {
+  kdgr_camera k;
+  for (int i = 0; i < 3; ++i) {
+    k.pos[i] = c.pos[i];
+    k.uaxis[i] = c.uaxis[i];
+    k.vaxis[i] = c.vaxis[i];
+    k.naxis[i] = c.naxis[i];
+  }
+  k.fovy = c.fovy;
+  k.aspect = c.aspect;
+  k.near_c = c.near_c;
+  return k;
+}
+
+}  // namespace
+
+bool initCuda() {
+  const int rc = kdgr_init(0);
+  if (rc != KDGR_OK) {
+    fprintf(stderr, "[CUDA Init] %s\n", kdgr_last_error());
+    return false;
+  }
+  return true;
+}
+
+void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vector<Gaussian>& gaussians) {
+  static_assert(sizeof(Gaussian) == 256, "Gaussian must be the reference's 256-byte record");
+  std::lock_guard<std::mutex> lk(g_mu);
+  const KdTree* t = object.kd_tree;
+  if (!t || gaussians.empty()) {
+    fprintf(stderr, "[CUDA Error] Kd-tree or Gaussian data is empty.\n");
+    return;
+  }
+  if (g_scene) {
+    kdgr_scene_destroy(g_scene);
+    g_scene = nullptr;
+  }
+  // CompositeObject.AABB is (xmin, xmax, ymin, ymax, zmin, zmax); the scene
+  // takes the .kdt order (xmin, ymin, zmin, xmax, ymax, zmax)
+  const float aabb[6] = {object.AABB[0], object.AABB[2], object.AABB[4],
+                         object.AABB[1], object.AABB[3], object.AABB[5]};
+  const int rc = kdgr_scene_create(reinterpret_cast<const uint32_t*>(t->tree), (uint32_t)t->tree_node_count,
+                                   t->prim_offset_list, (uint32_t)t->prim_offset_count, aabb,
+                                   reinterpret_cast<const float*>(gaussians.data()), (uint32_t)gaussians.size(),
+                                   KDGR_SCALES_INVERTED | KDGR_FORM_EXACT, &g_scene);
+  if (rc != KDGR_OK) {
+    fprintf(stderr, "[CUDA Error] setup failed: %s\n", kdgr_last_error());
+    g_scene = nullptr;
+  }
+}
+
+float renderGaussianWithCudaFrame(const Camera& camera, int width, int height, float* d_framebuffer,
+                                  cudaStream_t stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_scene) {
+    fprintf(stderr, "[CUDA Error] renderGaussianWithCudaFrame before renderGaussianWithCudaSetup\n");
+    return 0.f;
+  }
+  const kdgr_camera cam = to_camera(camera);
+  float ms = 0.f;
+  const int rc = kdgr_render(g_scene, &cam, width, height, d_framebuffer, nullptr, nullptr, (void*)stream, &ms);
+  if (rc != KDGR_OK) {
+    fprintf(stderr, "[CUDA Error] render failed: %s\n", kdgr_last_error());
+    return 0.f;
+  }
+  g_last_cam = cam;
+  g_last_w = width;
+  g_last_h = height;
+  g_have_frame = true;
+  return ms > 0.f ? 1000.0f / ms : 0.f;
+}
+
+void warmUp(float* d_framebuffer, cudaStream_t stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_scene || !g_have_frame) return;
+  float ms = 0.f;
+  if (kdgr_render(g_scene, &g_last_cam, g_last_w, g_last_h, d_framebuffer, nullptr, nullptr, (void*)stream, &ms) ==
+      KDGR_OK)
+    printf("WarmUp: %f\n", ms > 0.f ? 1000.0f / ms : 0.f);
+}
+
+void cleanupCudaResources() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_scene) kdgr_scene_destroy(g_scene);
+  g_scene = nullptr;
+  g_have_frame = false;
+  if (g_have_tree) kdgr_tree_free(&g_tree);
+  g_have_tree = false;
+}
+
+int read_kd_tree_from_file(CompositeObject* object, const char* filename, int dump_format) {
+  if (!object || !filename) return 0;
+  if (dump_format != KD_TREE_DUMP_IN_BINARY) {
+    fprintf(stderr, "read_kd_tree_from_file: only the binary .kdt format is supported\n");
+    return 0;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  kdgr_tree t;
+  if (kdgr_read_kdt(filename, &t) != KDGR_OK) {
+    fprintf(stderr, "%s kd-tree File Load Error! (%s)\n", filename, kdgr_last_error());
+    return 0;
+  }
+  if (g_have_tree) kdgr_tree_free(&g_tree);
+  g_tree = t;
+  g_have_tree = true;
+  static KdTree kt;
+  kt.tree = reinterpret_cast<KdTreeNode*>(g_tree.nodes);
+  kt.tree_node_count = (int)g_tree.n_nodes;
+  kt.prim_offset_list = g_tree.offsets;
+  kt.prim_offset_count = (int)g_tree.n_offsets;
+  // .kdt header order (xmin, ymin, zmin, xmax, ymax, zmax) -> AABB[XMIN..ZMAX]
+  object->AABB[0] = g_tree.aabb[0];
+  object->AABB[2] = g_tree.aabb[1];
+  object->AABB[4] = g_tree.aabb[2];
+  object->AABB[1] = g_tree.aabb[3];
+  object->AABB[3] = g_tree.aabb[4];
+  object->AABB[5] = g_tree.aabb[5];
+  memcpy(kt.AABB, object->AABB, sizeof(kt.AABB));
+  object->kd_tree = &kt;
+  return 1;
+}
