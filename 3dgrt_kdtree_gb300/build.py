@@ -28,6 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_UNITS = {
     "render_exact.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "render_fast.cu": [],
+    "kdgr_noalloc.cu": [],
 }
 CPP_UNITS = ["kdbuild.cpp", "kdgr_tree_api.cpp", "kdgr_api.cpp", "kdgr_batch_api.cpp", "kdgr_reference_api.cpp"]
 

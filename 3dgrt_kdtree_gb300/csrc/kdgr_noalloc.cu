@@ -1,0 +1,102 @@
+// kdgr_noalloc.cu -- kdgr_render_batch_noalloc: the batched render call for
+// callers that cannot allocate device memory.
+//
+// kdgr_render_batch takes its scratch -- the per-view table the persistent
+// kernel reads and the atomic work-queue counter -- from the stream-ordered
+// allocator on every call.  Some callers must not allocate at all: a host
+// application that owns the whole device-memory budget and forbids libraries
+// from taking more (or runs under a hard cap that an allocation could
+// exceed), or a frame loop that must not enter the allocator, where an
+// allocation can synchronise or fail from fragmentation at the worst moment.
+// For them this entry point renders with the same kernel, but its scratch
+// lives in one fixed, file-scope __device__ array: 24 KiB, enough for 256
+// views.  Every GPU that loads the library holds that array until the
+// process exits.
+//
+// Host code cannot pass the array's name to a kernel: on the host that name
+// is only a stand-in, not a device address.  The first call on each device
+// therefore asks the runtime for the array's device address
+// (cudaGetSymbolAddress) with that device current and caches it; make that
+// first call before any stream capture.  All calls share the array and it
+// keeps the previous call's contents: each call rewrites the view table and
+// zeroes the queue counter before its launch, so calls must not overlap on
+// the GPU (issue them on one stream, or order them) -- overlapping calls race
+// on the table and the counter.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "kdgr_internal.h"
+#include "scene.h"
+
+namespace kdgr {
+namespace {
+
+constexpr int kNoAllocMaxViews = 256;
+constexpr size_t kTableBytes = kNoAllocMaxViews * sizeof(ViewDesc);  // 22528
+constexpr size_t kCounterOffset = (kTableBytes + 255) & ~size_t(255);
+constexpr size_t kScratchBytes = 24 * 1024;
+static_assert(kCounterOffset + sizeof(uint32_t) <= kScratchBytes, "no-alloc scratch too small");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_addr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (set up once).
+cudaError_t scratch_address(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_addr[dev] = p;
+  }
+  *out = g_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace kdgr
+
+using namespace kdgr;
+
+extern "C" int kdgr_render_batch_noalloc(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb,
+                                         float* alpha, float* depth, const kdgr_batch_config* cfg, void* stream) {
+  if (!s || !views || n_views <= 0 || !rgb) {
+    set_error("kdgr_render_batch_noalloc: null scene/views/output or no views");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (n_views > kNoAllocMaxViews) {
+    set_error("kdgr_render_batch_noalloc: " + std::to_string(n_views) + " views exceed the fixed scratch limit of " +
+              std::to_string(kNoAllocMaxViews) + " views");
+    return KDGR_ERR_LIMIT;
+  }
+  kdgr_batch_config c;
+  if (cfg) c = *cfg;
+  else kdgr_batch_config_default(&c);
+  int rc = check_batch_config(s, c);
+  if (rc != KDGR_OK) return rc;
+  ViewDesc table[kNoAllocMaxViews];
+  uint32_t totals[3] = {0, 0, 0};
+  rc = fill_view_table(views, n_views, table, totals);
+  if (rc != KDGR_OK) return rc;
+  void* base = nullptr;
+  cudaError_t e = scratch_address(&base);
+  if (e != cudaSuccess) return cuda_fail(e, "kdgr_render_batch_noalloc: scratch address");
+  ViewDesc* d_views = static_cast<ViewDesc*>(base);
+  uint32_t* d_queue = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(base) + kCounterOffset);
+  const cudaStream_t st = (cudaStream_t)stream;
+  // pageable source: the copy is staged before the call returns
+  e = cudaMemcpyAsync(d_views, table, (size_t)n_views * sizeof(ViewDesc), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = launch_batch(s, c, d_views, n_views, totals, rgb, alpha, depth, d_queue, st);
+  if (e != cudaSuccess) return cuda_fail(e, "kdgr_render_batch_noalloc");
+  return KDGR_OK;
+}

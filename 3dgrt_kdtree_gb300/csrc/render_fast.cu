@@ -559,6 +559,38 @@ int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& 
   return KDGR_OK;
 }
 
+// As make_view_table, into a caller-provided array of n_views entries (no
+// allocation).
+int fill_view_table(const kdgr_view* views, int n_views, ViewDesc* out, uint32_t totals[3]) {
+  uint64_t wbase = 0, cbase = 0;
+  for (int v = 0; v < n_views; ++v) {
+    const kdgr_view& kv = views[v];
+    if (kv.width <= 0 || kv.height <= 0) {
+      set_error("view " + std::to_string(v) + " has an empty image");
+      return KDGR_ERR_INVALID_ARG;
+    }
+    ViewDesc& d = out[v];
+    d.cam = make_caminfo(kv.cam, kv.width, kv.height);
+    d.W = kv.width;
+    d.H = kv.height;
+    d.wt_x = (uint32_t)((kv.width + kTileW - 1) / kTileW);
+    d.wt_base = (uint32_t)wbase;
+    d.cb_x = (uint32_t)((kv.width + kBlockW - 1) / kBlockW);
+    d.cb_base = (uint32_t)cbase;
+    d.out_off = kv.out_offset;
+    wbase += (uint64_t)d.wt_x * (uint64_t)((kv.height + kTileH - 1) / kTileH);
+    cbase += (uint64_t)d.cb_x * (uint64_t)((kv.height + kBlockH - 1) / kBlockH);
+    if (wbase > 0xF0000000ull) {
+      set_error("batch too large: more than 2^32 tiles");
+      return KDGR_ERR_LIMIT;
+    }
+  }
+  totals[0] = (uint32_t)wbase;
+  totals[1] = (uint32_t)cbase;
+  totals[2] = 0;
+  return KDGR_OK;
+}
+
 int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
   if (c.precision && !(s->forms & KDGR_FORM_PACKED)) {
     set_error("precision form requested but the scene was created without KDGR_FORM_PACKED");

@@ -73,6 +73,7 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
 // Batched rendering (render_fast.cu).
 // totals: 8x4 tiles, 16x8 blocks and 32x16 super-blocks over all views.
 int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]);
+int fill_view_table(const kdgr_view* views, int n_views, ViewDesc* out, uint32_t totals[3]);
 int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c);
 cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewDesc* d_views, int n_views,
                          const uint32_t totals[3], float* rgb, float* alpha, float* depth, uint32_t* queue,

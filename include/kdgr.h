@@ -201,6 +201,18 @@ void kdgr_batch_config_default(kdgr_batch_config* cfg);
 int kdgr_render_batch(kdgr_scene_t scene, const kdgr_view* views, int n_views, float* d_rgb, float* d_alpha,
                       float* d_depth, const kdgr_batch_config* cfg, void* stream, float* ms_out);
 
+/* kdgr_render_batch for callers that cannot allocate device memory (a host
+ * that owns the whole device-memory budget, or a frame loop that must never
+ * enter the allocator).  No counterpart in the reference.  Same kernel and
+ * results as kdgr_render_batch, but the scratch (view table + work-queue
+ * counter) is a fixed 24 KiB file-scope device array, so at most 256 views
+ * per call (KDGR_ERR_LIMIT beyond); it calls no device allocator.  The first
+ * call on a device looks up the array's device address -- make it before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU race;
+ * issue them on one stream.  Asynchronous on `stream`. */
+int kdgr_render_batch_noalloc(kdgr_scene_t scene, const kdgr_view* views, int n_views, float* d_rgb,
+                              float* d_alpha, float* d_depth, const kdgr_batch_config* cfg, void* stream);
+
 /* One view through the batch kernel with the default configuration;
  * precision 0 = FP32 arrays, 1 = packed BF16/FP16 arrays. */
 int kdgr_render_fast(kdgr_scene_t scene, const kdgr_camera* cam, int width, int height, float* d_rgb,

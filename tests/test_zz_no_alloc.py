@@ -1,0 +1,75 @@
+"""kdgr_render_batch_noalloc, the batched render call for callers that cannot
+allocate device memory (a host that owns the whole device-memory budget, or a
+frame loop that must never enter the allocator).
+
+It renders with the same kernel as kdgr_render_batch, but takes its scratch
+(view table and work-queue counter) from a fixed file-scope device array
+instead of the allocator.  Called here through the C ABI, twice in a row with
+different view sets -- the shared array keeps the previous call's contents,
+so each call must rewrite the table and zero the counter -- and checked
+against kdgr_render_batch within the parity tolerance of the tests (1e-5
+absolute).  The file sorts last so that a run stopping at the first failure
+has already run every other test; it also passes alone in a fresh process.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+MAX_VIEWS = 256
+
+
+def _noalloc(pkg):
+    L = pkg.capi.lib()
+    F = pkg.renderer
+    fn = L.kdgr_render_batch_noalloc
+    vp = ctypes.c_void_p
+    fn.argtypes = [vp, ctypes.POINTER(F.View), ctypes.c_int, vp, vp, vp, ctypes.POINTER(F.BatchConfig), vp]
+    fn.restype = ctypes.c_int
+    return fn
+
+
+def test_noalloc_matches_batch_two_calls(pkg, cuda, fixtures):
+    F = pkg.renderer
+    fx = fixtures["dense800"]
+    scene = F.Scene(fx.tree, fx.rec)
+    fn = _noalloc(pkg)
+    stream = torch.cuda.current_stream().cuda_stream
+    view_sets = [
+        pkg.scenes.sphere_cameras(5, seed=21, resolutions=[(48, 40), (33, 17)]),
+        pkg.scenes.sphere_cameras(3, seed=22, resolutions=[(64, 48)]),
+    ]
+    for cams in view_sets:
+        views, total, _ = F.make_views(cams)
+        ref_rgb = torch.zeros(total * 3, device=cuda)
+        ref_a = torch.zeros(total, device=cuda)
+        scene.render_batch(views, len(cams), ref_rgb, ref_a)
+        rgb = torch.full((total * 3,), -1.0, device=cuda)
+        alpha = torch.full((total,), -1.0, device=cuda)
+        rc = fn(scene.handle, views, len(cams), rgb.data_ptr(), alpha.data_ptr(), None, None, stream)
+        assert rc == 0, pkg.capi.lib().kdgr_last_error()
+        torch.cuda.synchronize()
+        assert scene.status() == 0
+        np.testing.assert_allclose(rgb.cpu().numpy(), ref_rgb.cpu().numpy(), rtol=0, atol=TOL)
+        np.testing.assert_allclose(alpha.cpu().numpy(), ref_a.cpu().numpy(), rtol=0, atol=TOL)
+        assert float(ref_a.max()) > 0.0  # the views see the scene
+    scene.close()
+
+
+def test_noalloc_rejects_more_views_than_its_scratch_holds(pkg, cuda, fixtures):
+    F = pkg.renderer
+    fx = fixtures["uniform2k"]
+    scene = F.Scene(fx.tree, fx.rec)
+    fn = _noalloc(pkg)
+    cams = [(pkg.scenes.front_camera(8, 8), 8, 8)] * (MAX_VIEWS + 1)
+    views, total, _ = F.make_views(cams)
+    rgb = torch.zeros(total * 3, device=cuda)
+    rc = fn(scene.handle, views, len(cams), rgb.data_ptr(), None, None, None,
+            torch.cuda.current_stream().cuda_stream)
+    assert rc == 10  # KDGR_ERR_LIMIT
+    assert b"256" in pkg.capi.lib().kdgr_last_error()
+    scene.close()
