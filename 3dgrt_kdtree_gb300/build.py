@@ -30,7 +30,8 @@ CU_UNITS = {
     "render_fast.cu": [],
     "kdgr_noalloc.cu": [],
 }
-CPP_UNITS = ["kdbuild.cpp", "kdgr_tree_api.cpp", "kdgr_api.cpp", "kdgr_batch_api.cpp", "kdgr_reference_api.cpp"]
+CPP_UNITS = ["kdbuild.cpp", "kdgr_tree_api.cpp", "kdgr_api.cpp", "kdgr_batch_api.cpp", "kdgr_reference_api.cpp",
+             "kdgr_server.cpp"]
 
 
 def _cuda_home() -> str:

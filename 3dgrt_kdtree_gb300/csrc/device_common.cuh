@@ -72,6 +72,8 @@ struct ViewDesc {
   uint32_t wt_x, wt_base;  // 8x4 tiles per row; first global tile of the view
   uint32_t cb_x, cb_base;  // 16x8 blocks per row; first global block
   uint64_t out_off;
+  uint32_t scene;          // scene slot (multi-scene launches of the serving loop)
+  uint32_t pad;
 };
 
 __host__ __device__ inline uint64_t fnv_add(uint64_t h, uint32_t v) {

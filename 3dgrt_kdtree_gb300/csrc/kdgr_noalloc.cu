@@ -9,7 +9,7 @@
 // exceed), or a frame loop that must not enter the allocator, where an
 // allocation can synchronise or fail from fragmentation at the worst moment.
 // For them this entry point renders with the same kernel, but its scratch
-// lives in one fixed, file-scope __device__ array: 24 KiB, enough for 256
+// lives in one fixed, file-scope __device__ array: 32 KiB, enough for 256
 // views.  Every GPU that loads the library holds that array until the
 // process exits.
 //
@@ -34,9 +34,9 @@ namespace kdgr {
 namespace {
 
 constexpr int kNoAllocMaxViews = 256;
-constexpr size_t kTableBytes = kNoAllocMaxViews * sizeof(ViewDesc);  // 22528
+constexpr size_t kTableBytes = kNoAllocMaxViews * sizeof(ViewDesc);  // 24576
 constexpr size_t kCounterOffset = (kTableBytes + 255) & ~size_t(255);
-constexpr size_t kScratchBytes = 24 * 1024;
+constexpr size_t kScratchBytes = 32 * 1024;
 static_assert(kCounterOffset + sizeof(uint32_t) <= kScratchBytes, "no-alloc scratch too small");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];

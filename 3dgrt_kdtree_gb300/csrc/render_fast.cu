@@ -40,7 +40,7 @@
 
 namespace kdgr {
 
-static_assert(sizeof(ViewDesc) == 88, "ViewDesc layout (bench.py counts 88 B per view)");
+static_assert(sizeof(ViewDesc) == 96, "ViewDesc layout (bench.py counts 96 B per view)");
 
 namespace {
 
@@ -467,6 +467,34 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
   }
 }
 
+// Multi-scene form of the CTA-block schedule for the serving loop: every view
+// names a scene slot and the CTA renders each block against that slot's
+// arrays (scenes[] in device memory).  One persistent launch serves the
+// requests of all resident scenes queued in a tick.
+template <bool PACKED>
+__global__ void __launch_bounds__(kThreads, 6) k_render_multi(const FastView* __restrict__ scenes,
+                                                              const ViewDesc* __restrict__ views, int n_views,
+                                                              uint32_t total_items, float* __restrict__ rgb,
+                                                              uint32_t* queue, uint32_t* status) {
+  __shared__ uint32_t s_id[kStack][kThreads];
+  __shared__ float s_t[kStack][kThreads];
+  __shared__ uint32_t s_work;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  while (true) {
+    __syncthreads();
+    if (tid == 0) s_work = atomicAdd(queue, 1u);
+    __syncthreads();
+    const uint32_t item = s_work;
+    if (item >= total_items) break;
+    const ViewDesc& V = views[find_view(views, n_views, item, KDGR_SCHED_CTA_BLOCKS)];
+    const FastView& S = scenes[__ldg(&V.scene)];
+    const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
+    const int x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
+    const int y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
+    render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, nullptr, nullptr, status);
+  }
+}
+
 // FP64 precompute of M = diag(1/s) R^T and b = M mu for anisotropic
 // Gaussians (upload time only).  src: 10 floats per entry (inverse scale x3,
 // quaternion w,x,y,z, mean x3).
@@ -546,6 +574,8 @@ int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& 
     d.cb_x = (uint32_t)((kv.width + kBlockW - 1) / kBlockW);
     d.cb_base = (uint32_t)cbase;
     d.out_off = kv.out_offset;
+    d.scene = 0;
+    d.pad = 0;
     wbase += (uint64_t)d.wt_x * (uint64_t)((kv.height + kTileH - 1) / kTileH);
     cbase += (uint64_t)d.cb_x * (uint64_t)((kv.height + kBlockH - 1) / kBlockH);
     if (wbase > 0xF0000000ull) {
@@ -578,6 +608,8 @@ int fill_view_table(const kdgr_view* views, int n_views, ViewDesc* out, uint32_t
     d.cb_x = (uint32_t)((kv.width + kBlockW - 1) / kBlockW);
     d.cb_base = (uint32_t)cbase;
     d.out_off = kv.out_offset;
+    d.scene = 0;
+    d.pad = 0;
     wbase += (uint64_t)d.wt_x * (uint64_t)((kv.height + kTileH - 1) / kTileH);
     cbase += (uint64_t)d.cb_x * (uint64_t)((kv.height + kBlockH - 1) / kBlockH);
     if (wbase > 0xF0000000ull) {
@@ -705,5 +737,17 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
 }
 
 int batch_sms() { return num_sms(); }
+
+cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* d_views, int n_views,
+                         uint32_t total_blocks, float* rgb, uint32_t* queue, uint32_t* status, cudaStream_t st) {
+  auto fn = packed ? k_render_multi<true> : k_render_multi<false>;
+  int occ = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  uint64_t blocks = (uint64_t)num_sms() * (occ > 0 ? occ : 1);
+  if (blocks > total_blocks) blocks = total_blocks > 0 ? total_blocks : 1;
+  fn<<<(unsigned)blocks, kThreads, 0, st>>>(d_scenes, d_views, n_views, total_blocks, rgb, queue, status);
+  return cudaGetLastError();
+}
 
 }  // namespace kdgr

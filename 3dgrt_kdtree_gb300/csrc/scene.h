@@ -79,6 +79,10 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
                          const uint32_t totals[3], float* rgb, float* alpha, float* depth, uint32_t* queue,
                          cudaStream_t st);
 int batch_sms();
+// Multi-scene persistent launch (CTA-block schedule) for the serving loop;
+// views[].scene indexes d_scenes.
+cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* d_views, int n_views,
+                         uint32_t total_blocks, float* rgb, uint32_t* queue, uint32_t* status, cudaStream_t st);
 // Scale ratio above which a Gaussian's factors come from the FP64 precompute.
 constexpr double kAnisoRatio = 1e3;
 }  // namespace kdgr

@@ -54,8 +54,37 @@ class BatchConfig(ctypes.Structure):
         return c
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("arena_bytes", ctypes.c_uint64),
+                ("max_views_per_launch", ctypes.c_int32), ("lanes", ctypes.c_int32), ("precision", ctypes.c_int32)]
+
+
+class RequestStats(ctypes.Structure):
+    _fields_ = [("latency_ms", ctypes.c_double), ("queue_ms", ctypes.c_double), ("rays", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("cancelled", ctypes.c_uint64), ("queued", ctypes.c_uint64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("mrays_per_s", ctypes.c_double), ("rays", ctypes.c_uint64),
+                ("launches", ctypes.c_uint64), ("views_launched", ctypes.c_uint64),
+                ("max_views_per_launch", ctypes.c_uint64), ("resident_bytes", ctypes.c_uint64)]
+
+
 vp = ctypes.c_void_p
 capi._EXTRA_SIGS.update({
+    "kdgr_server_config_default": [ctypes.POINTER(ServerConfig)],
+    "kdgr_server_create": [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)],
+    "kdgr_server_add_scene": [vp, vp, ctypes.c_uint32, vp, ctypes.c_uint32, vp, vp, ctypes.c_uint32, ctypes.c_uint32,
+                              ctypes.POINTER(ctypes.c_int)],
+    "kdgr_server_remove_scene": [vp, ctypes.c_int],
+    "kdgr_server_submit": [vp, ctypes.c_int, ctypes.POINTER(View), ctypes.c_int, vp,
+                           ctypes.POINTER(ctypes.c_uint64)],
+    "kdgr_server_wait": [vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(RequestStats)],
+    "kdgr_server_cancel": [vp, ctypes.c_uint64],
+    "kdgr_server_stats_get": [vp, ctypes.POINTER(ServerStats)],
+    "kdgr_server_reset_stats": [vp],
+    "kdgr_server_destroy": [vp],
     "kdgr_init": [ctypes.c_int],
     "kdgr_scene_create": [vp, ctypes.c_uint32, vp, ctypes.c_uint32, vp, vp, ctypes.c_uint32, ctypes.c_uint32,
                           ctypes.POINTER(vp)],
@@ -211,6 +240,83 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "handle", None):
             capi.lib().kdgr_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """The serving loop (kdgr_server_*): resident scenes under an HBM budget,
+    continuous batching of requests into persistent multi-scene launches."""
+
+    def __init__(self, hbm_budget_bytes: int | None = None, arena_bytes: int | None = None,
+                 max_views_per_launch: int | None = None, lanes: int | None = None, precision: int = 0):
+        L = capi.lib()
+        c = ServerConfig()
+        L.kdgr_server_config_default(ctypes.byref(c))
+        if hbm_budget_bytes is not None:
+            c.hbm_budget_bytes = hbm_budget_bytes
+        if arena_bytes is not None:
+            c.arena_bytes = arena_bytes
+        if max_views_per_launch is not None:
+            c.max_views_per_launch = max_views_per_launch
+        if lanes is not None:
+            c.lanes = lanes
+        c.precision = precision
+        h = ctypes.c_void_p()
+        capi.check(L.kdgr_server_create(ctypes.byref(c), ctypes.byref(h)), "kdgr_server_create")
+        self.handle = h
+        self.config = c
+
+    def add_scene(self, tree: KdTree, gaussians: np.ndarray, scales_inverted: bool = False) -> int:
+        nodes = np.ascontiguousarray(tree.nodes, dtype=np.uint32)
+        offs = np.ascontiguousarray(tree.offsets, dtype=np.uint32)
+        aabb = np.ascontiguousarray(tree.aabb, dtype=np.float32)
+        rec = np.ascontiguousarray(gaussians, dtype=np.float32)
+        slot = ctypes.c_int()
+        capi.check(capi.lib().kdgr_server_add_scene(self.handle, nodes.ctypes.data, nodes.shape[0],
+                                                    offs.ctypes.data if offs.size else None, offs.shape[0],
+                                                    aabb.ctypes.data, rec.ctypes.data, rec.shape[0],
+                                                    SCALES_INVERTED if scales_inverted else 0, ctypes.byref(slot)),
+                   "kdgr_server_add_scene")
+        return int(slot.value)
+
+    def remove_scene(self, slot: int) -> None:
+        capi.check(capi.lib().kdgr_server_remove_scene(self.handle, slot), "kdgr_server_remove_scene")
+
+    def submit(self, slot: int, views, n_views: int, host_rgb) -> int:
+        """host_rgb: a (pinned) CPU torch tensor or numpy array with 3 floats per pixel."""
+        ptr = host_rgb.data_ptr() if hasattr(host_rgb, "data_ptr") else host_rgb.ctypes.data
+        t = ctypes.c_uint64()
+        capi.check(capi.lib().kdgr_server_submit(self.handle, slot, views, n_views, ptr, ctypes.byref(t)),
+                   "kdgr_server_submit")
+        return int(t.value)
+
+    def wait(self, ticket: int, timeout_ms: int = 60_000) -> tuple:
+        """Returns (status, stats dict); status 0 = done, 9 = cancelled, 7 = timeout."""
+        st = RequestStats()
+        rc = capi.lib().kdgr_server_wait(self.handle, ticket, timeout_ms, ctypes.byref(st))
+        return rc, {"latency_ms": st.latency_ms, "queue_ms": st.queue_ms, "rays": int(st.rays)}
+
+    def cancel(self, ticket: int) -> int:
+        return capi.lib().kdgr_server_cancel(self.handle, ticket)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        capi.check(capi.lib().kdgr_server_stats_get(self.handle, ctypes.byref(s)), "kdgr_server_stats_get")
+        return {k: (float(getattr(s, k)) if isinstance(getattr(s, k), float) else int(getattr(s, k)))
+                for k, _ in s._fields_}
+
+    def reset_stats(self) -> None:
+        capi.lib().kdgr_server_reset_stats(self.handle)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            capi.lib().kdgr_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -222,7 +222,7 @@ def run_ours(args, rank: int, world: int):
         e2e_step()
     ms_e2e = timed_loop(e2e_step, args.steps)
     e2e_step_ms = sum(ms_e2e) / len(ms_e2e)
-    view_bytes = 88 * len(cams)  # ViewDesc table (88 B per view) copied host->device by kdgr_render_batch
+    view_bytes = 96 * len(cams)  # ViewDesc table (96 B per view) copied host->device by kdgr_render_batch
     e2e = {"value": rays * world / (e2e_step_ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": view_bytes,
            "d2h_bytes_per_step": int(host.numel() * 4), "ms_per_step": e2e_step_ms,
            "path": "kdgr_render_batch (C ABI) + D2H of the RGB frame"}
@@ -285,6 +285,129 @@ def run_ours(args, rank: int, world: int):
     batch.close()
     scene.close()
     return out
+
+
+# ------------------------------------------------------------------ serving
+def poisson_requests(rate: float, seconds: float, n_scenes: int, seed: int):
+    """[(arrival_s, scene, [(Camera, W, H)])]: Poisson arrivals, 1-16 views per
+    request, each view's resolution uniform over the four, scene uniform."""
+    import importlib as _il
+    sc = _il.import_module("3dgrt_kdtree_gb300.scenes")
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            return out
+        nv = int(rng.integers(1, 17))
+        cams = []
+        for _ in range(nv):
+            w, h = sc.RESOLUTIONS[int(rng.integers(0, 4))]
+            d = rng.normal(0.0, 1.0, 3)
+            d /= np.linalg.norm(d)
+            cams.append((sc.look_at(d * rng.uniform(2.0, 4.0), aspect=w / h), w, h))
+        out.append((t, int(rng.integers(0, n_scenes)), cams))
+
+
+def run_serving(args):
+    """Four resident scenes (0.5M/1M/2M/3M cluster+shell, seeds 1-4) under a
+    60 GB budget; Poisson request streams at each rate, served by the
+    continuous-batching server, and by the plain per-request path (one
+    request at a time, one plain-kernel launch per view) for comparison."""
+    import threading
+    import torch
+    pkg = importlib.import_module("3dgrt_kdtree_gb300")
+    F = pkg.renderer
+    F.init(0)
+    sizes = [500_000, 1_000_000, 2_000_000, 3_000_000]
+    srv = F.Server(hbm_budget_bytes=60 << 30, arena_bytes=8 << 30, lanes=3, max_views_per_launch=256)
+    plain_scenes, slots = [], []
+    t0 = time.time()
+    for i, n in enumerate(sizes):
+        rec = pkg.scenes.cluster_shell(n, seed=i + 1)
+        tree = pkg.kdtree.build(rec)
+        slots.append(srv.add_scene(tree, rec))
+        plain_scenes.append(F.Scene(tree, rec, forms=F.FORM_EXACT))
+    log(f"[bench] serving: 4 scenes built and resident in {time.time() - t0:.1f}s, "
+        f"{srv.stats()['resident_bytes'] / 1e9:.1f} GB of the 60 GB budget")
+    rates = [float(r) for r in args.rates.split(",")]
+    results = {}
+    for rate in rates:
+        reqs = poisson_requests(rate, args.serve_seconds, len(sizes), seed=int(rate))
+        rays = sum(w * h for _, _, cams in reqs for _, w, h in cams)
+        # served
+        srv.reset_stats()
+        bufs, tickets = [], []
+        start = time.time()
+        for arr, scene, cams in reqs:
+            now = time.time() - start
+            if arr > now:
+                time.sleep(arr - now)
+            views, total, _ = F.make_views(cams)
+            buf = np.empty(total * 3, np.float32)
+            bufs.append(buf)
+            tickets.append(srv.submit(slots[scene], views, len(cams), buf))
+        for t in tickets:
+            rc, _ = srv.wait(t, timeout_ms=600_000)
+            assert rc == 0
+        st = srv.stats()
+        # plain path: FIFO, one request at a time, plain kernel per view
+        dev = torch.device("cuda:0")
+        q, lat, lock = [], [], threading.Lock()
+        done_evt = threading.Event()
+
+        def worker():
+            stream = torch.cuda.current_stream(dev)
+            while True:
+                with lock:
+                    item = q.pop(0) if q else None
+                if item is None:
+                    if done_evt.is_set():
+                        return
+                    time.sleep(0.0005)
+                    continue
+                arr_abs, scene, cams = item
+                for cam, w, h in cams:
+                    out = torch.empty(w * h * 3, device=dev)
+                    plain_scenes[scene].render(cam, w, h, out)
+                    out.cpu()
+                stream.synchronize()
+                lat.append(1e3 * (time.time() - arr_abs))
+
+        th = threading.Thread(target=worker)
+        th.start()
+        start = time.time()
+        for arr, scene, cams in reqs:
+            now = time.time() - start
+            if arr > now:
+                time.sleep(arr - now)
+            with lock:
+                q.append((start + arr, scene, cams))
+        done_evt.set()
+        th.join()
+        plain_wall = time.time() - start
+        lat.sort()
+        pct = lambda v, p: v[min(len(v) - 1, int(p * (len(v) - 1) + 0.5))]
+        results[str(int(rate))] = {
+            "requests": len(reqs), "rays": int(rays),
+            "served": {"p50_ms": round(st["p50_ms"], 2), "p99_ms": round(st["p99_ms"], 2),
+                       "mean_ms": round(st["mean_ms"], 2), "mrays_per_s": round(st["mrays_per_s"], 1),
+                       "launches": st["launches"], "max_views_per_launch": st["max_views_per_launch"]},
+            "plain": {"p50_ms": round(pct(lat, 0.5), 2), "p99_ms": round(pct(lat, 0.99), 2),
+                      "mrays_per_s": round(rays / plain_wall / 1e6, 1)},
+        }
+        log(f"[bench] rate {rate}: {results[str(int(rate))]}")
+    key = "50" if "50" in results else list(results)[0]
+    srv.close()
+    return {
+        "metric": f"served p99 latency at {key} req/s", "value": results[key]["served"]["p99_ms"], "unit": "ms",
+        "n_gpus": 1, "steps": len(rates), "warmup": 0, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "4 resident cluster+shell scenes (0.5M/1M/2M/3M), Poisson requests of 1-16 "
+                               "views at 256x256/640x480/1280x720/1920x1080, 60 GB budget",
+                   "form": "continuous-batching server, 3 lanes", "seconds_per_rate": args.serve_seconds},
+        "serving": results,
+    }
 
 
 # ------------------------------------------------------------------ CPU arm
@@ -350,7 +473,10 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="scale", choices=["scale", "small", "mid", "batching", "precision"])
+    ap.add_argument("--config", default="scale",
+                    choices=["scale", "small", "mid", "batching", "precision", "serving"])
+    ap.add_argument("--rates", default="25,50,100", help="serving: Poisson request rates (req/s)")
+    ap.add_argument("--serve-seconds", type=float, default=4.0, help="serving: arrivals per rate")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: default kernel config, no L2-flush buffer, no e2e/plain/CPU legs")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -370,7 +496,7 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    out = run_ours(args, rank, world)
+    out = run_serving(args) if args.config == "serving" else run_ours(args, rank, world)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -205,7 +205,7 @@ int kdgr_render_batch(kdgr_scene_t scene, const kdgr_view* views, int n_views, f
  * that owns the whole device-memory budget, or a frame loop that must never
  * enter the allocator).  No counterpart in the reference.  Same kernel and
  * results as kdgr_render_batch, but the scratch (view table + work-queue
- * counter) is a fixed 24 KiB file-scope device array, so at most 256 views
+ * counter) is a fixed 32 KiB file-scope device array, so at most 256 views
  * per call (KDGR_ERR_LIMIT beyond); it calls no device allocator.  The first
  * call on a device looks up the array's device address -- make it before any
  * stream capture.  Calls share the array: calls that overlap on the GPU race;
@@ -233,6 +233,61 @@ int kdgr_batch_destroy(kdgr_batch_t batch);
  * line per variant. */
 int kdgr_autotune(kdgr_scene_t scene, const kdgr_view* views, int n_views, int precision, float* d_rgb,
                   kdgr_batch_config* best, char* report, int report_len);
+
+/* ------------------------------------------------------------ serving
+ * Serving form: scenes resident in HBM under an admission budget; render
+ * requests (a scene and 1..N views) are batched continuously -- everything
+ * queued when a lane (stream) frees up goes into one persistent multi-scene
+ * launch, so requests arriving while others are on the GPU overlap with them.
+ * Each ray depends only on its own view: a request's frames are identical
+ * alone and in any mix.  No reference counterpart. */
+typedef struct kdgr_server_s* kdgr_server_t;
+
+typedef struct {
+  uint64_t hbm_budget_bytes;     /* resident scenes + output arena may not exceed this */
+  uint64_t arena_bytes;          /* device output arena shared by in-flight requests */
+  int32_t max_views_per_launch;  /* views per persistent launch (and per request) */
+  int32_t lanes;                 /* launches in flight at once (streams), 1..8 */
+  int32_t precision;             /* 0: FP32 fast arrays; 1: BF16/FP16 arrays */
+} kdgr_server_config;
+
+typedef struct {
+  double latency_ms;  /* submit -> frames in the host buffer */
+  double queue_ms;    /* submit -> launch */
+  uint64_t rays;
+} kdgr_request_stats;
+
+typedef struct {
+  uint64_t completed, cancelled, queued;
+  double p50_ms, p99_ms, mean_ms, max_ms;
+  double mrays_per_s; /* rays completed / (last completion - first submit) */
+  uint64_t rays, launches, views_launched, max_views_per_launch;
+  uint64_t resident_bytes;
+} kdgr_server_stats;
+
+void kdgr_server_config_default(kdgr_server_config* cfg);
+int kdgr_server_create(const kdgr_server_config* cfg, kdgr_server_t* out);
+/* Upload a scene into a free slot; KDGR_ERR_BUDGET when it does not fit. */
+int kdgr_server_add_scene(kdgr_server_t server, const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets,
+                          uint32_t n_offsets, const float aabb[6], const float* gaussians, uint32_t n_gaussians,
+                          uint32_t flags, int* slot);
+/* Evict a scene: its queued requests finish with KDGR_ERR_CANCELLED; waits
+ * (at most 60 s) for launches that use it. */
+int kdgr_server_remove_scene(kdgr_server_t server, int slot);
+/* Queue a request.  host_rgb receives 3 floats per pixel at each view's
+ * out_offset (rows flipped per view); pinned memory copies fastest.  Returns
+ * KDGR_ERR_BUDGET when the request's output can never fit the arena. */
+int kdgr_server_submit(kdgr_server_t server, int slot, const kdgr_view* views, int n_views, float* host_rgb,
+                       uint64_t* ticket);
+/* Wait (at most timeout_ms) for a request; returns its status (KDGR_OK,
+ * KDGR_ERR_CANCELLED) or KDGR_ERR_TIMEOUT.  A finished ticket is released. */
+int kdgr_server_wait(kdgr_server_t server, uint64_t ticket, int timeout_ms, kdgr_request_stats* stats);
+/* Cancel a request that has not been launched yet. */
+int kdgr_server_cancel(kdgr_server_t server, uint64_t ticket);
+int kdgr_server_stats_get(kdgr_server_t server, kdgr_server_stats* out);
+int kdgr_server_reset_stats(kdgr_server_t server);
+/* Stop the loop (queued requests are cancelled, launches drain) and free everything. */
+int kdgr_server_destroy(kdgr_server_t server);
 
 /* ------------------------------------------------------------ per-ray trace
  * Written by the oracle-matching render path in trace mode (and by the CPU
