@@ -50,11 +50,12 @@ class BuildStats(ctypes.Structure):
 class RayTrace(ctypes.Structure):
     _fields_ = [("n_inner", ctypes.c_uint32), ("n_leaf", ctypes.c_uint32), ("n_cand", ctypes.c_uint32),
                 ("n_hit", ctypes.c_uint32), ("n_blend", ctypes.c_uint32), ("n_restart", ctypes.c_uint32),
+                ("n_found", ctypes.c_uint32), ("max_sort", ctypes.c_uint32),
                 ("h_leaf", ctypes.c_uint64), ("h_hit", ctypes.c_uint64), ("h_blend", ctypes.c_uint64)]
 
 
 TRACE_DTYPE = [("n_inner", "<u4"), ("n_leaf", "<u4"), ("n_cand", "<u4"), ("n_hit", "<u4"),
-               ("n_blend", "<u4"), ("n_restart", "<u4"), ("h_leaf", "<u8"), ("h_hit", "<u8"),
+               ("n_blend", "<u4"), ("n_restart", "<u4"), ("n_found", "<u4"), ("max_sort", "<u4"), ("h_leaf", "<u8"), ("h_hit", "<u8"),
                ("h_blend", "<u8")]
 
 _lib = None

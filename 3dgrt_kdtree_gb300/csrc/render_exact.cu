@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(kBlock) k_render_exact(ExactView S, CamInfo C,
 
   F3 acc = mk(0.f, 0.f, 0.f);
   float A = 0.f, D = 0.f;
-  uint32_t n_inner = 0, n_leaf = 0, n_cand = 0, n_hit = 0, n_blend = 0, n_restart = 0;
+  uint32_t n_inner = 0, n_leaf = 0, n_cand = 0, n_hit = 0, n_blend = 0, n_restart = 0, n_found = 0, max_sort = 0;
   uint64_t hl = kFnvInit, hh = kFnvInit, hb = kFnvInit;
 
   // BoundsRayIntersect (cudaRenderer.cu:379-399) with IEEE division
@@ -224,6 +224,7 @@ __global__ void __launch_bounds__(kBlock) k_render_exact(ExactView S, CamInfo C,
         }
         if (TRACE) n_cand += cnt;
         bool have_last = false, saturated = false;
+        uint32_t n_acc = 0;  // accepted in this leaf, counted on the first pass
         float last_t = 0.f;
         uint32_t last_i = 0;
         while (true) {
@@ -244,6 +245,7 @@ __global__ void __launch_bounds__(kBlock) k_render_exact(ExactView S, CamInfo C,
             }
             float t, g;
             if (!exact_test(o, d, S.test + 4ull * gid, t_near, t_far, &t, &g)) continue;
+            if (TRACE && !have_last) ++n_acc;
             if (have_last && !(t > last_t || (t == last_t && i > last_i))) continue;
             float ct = t, cg = g;
             uint32_t ci = i;
@@ -292,6 +294,10 @@ __global__ void __launch_bounds__(kBlock) k_render_exact(ExactView S, CamInfo C,
               break;
             }
           }
+          if (TRACE && !have_last) {
+            n_found += n_acc;
+            max_sort = max(max_sort, n_acc);
+          }
           if (saturated || !overflow) break;
           have_last = true;
           last_t = bt[K - 1];
@@ -332,6 +338,8 @@ finish:
       tr.n_hit = n_hit;
       tr.n_blend = n_blend;
       tr.n_restart = n_restart;
+      tr.n_found = n_found;
+      tr.max_sort = max_sort;
       tr.h_leaf = hl;
       tr.h_hit = hh;
       tr.h_blend = hb;

@@ -54,6 +54,14 @@ class BatchConfig(ctypes.Structure):
         return c
 
 
+class DebugStats(ctypes.Structure):
+    _fields_ = [("avg", ctypes.c_float * 6), ("total", ctypes.c_float * 6), ("max", ctypes.c_int32 * 6),
+                ("n_pixels", ctypes.c_uint32)]
+
+
+DEBUG_COUNTERS = ("node_visits", "leaf_visits", "intersection_tests", "hits_found", "blend_ops", "max_sort_size")
+
+
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("arena_bytes", ctypes.c_uint64),
                 ("max_views_per_launch", ctypes.c_int32), ("lanes", ctypes.c_int32), ("precision", ctypes.c_int32)]
@@ -103,6 +111,8 @@ capi._EXTRA_SIGS.update({
                           ctypes.POINTER(vp)],
     "kdgr_batch_run": [vp, vp],
     "kdgr_batch_destroy": [vp],
+    "kdgr_debug_report": [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_float,
+                          ctypes.POINTER(DebugStats)],
     "kdgr_autotune": [vp, ctypes.POINTER(View), ctypes.c_int, ctypes.c_int, vp, ctypes.POINTER(BatchConfig),
                       ctypes.c_char_p, ctypes.c_int],
 })
@@ -125,6 +135,26 @@ def _stream(stream) -> Optional[int]:
 
 def init(device: int = 0) -> None:
     capi.check(capi.lib().kdgr_init(device), "kdgr_init")
+
+
+def debug_report(trace, width: int, height: int, out_dir: Optional[str] = None,
+                 heat_max: float = 120.0) -> dict:
+    """The reference's HIT_AND_NODE_COUNT_DEBUG report over host traces (a
+    numpy array of capi.TRACE_DTYPE records in y*W + x order): returns
+    {counter: {"avg", "max", "total"}, "n_pixels"} and, with out_dir, writes
+    the reference's files there (kdgr_debug_report).  Host only."""
+    import numpy as np
+    tr = np.ascontiguousarray(trace)
+    if tr.dtype != np.dtype(capi.TRACE_DTYPE) or tr.size != width * height:
+        raise ValueError("trace must hold width*height records of capi.TRACE_DTYPE")
+    st = DebugStats()
+    capi.check(capi.lib().kdgr_debug_report(tr.ctypes.data, width, height,
+                                            out_dir.encode() if out_dir else None, heat_max, ctypes.byref(st)),
+               "kdgr_debug_report")
+    out = {name: {"avg": st.avg[k], "max": st.max[k], "total": st.total[k]}
+           for k, name in enumerate(DEBUG_COUNTERS)}
+    out["n_pixels"] = st.n_pixels
+    return out
 
 
 def make_views(cams: Sequence) -> tuple:
@@ -185,6 +215,18 @@ class Scene:
         capi.check(capi.lib().kdgr_render_trace(self.handle, ctypes.byref(c), width, height, _ptr(rgb),
                                                 _ptr(alpha), _ptr(depth), _ptr(trace), _stream(stream)),
                    "kdgr_render_trace")
+
+    def debug_counters(self, cam, width: int, height: int):
+        """Per-pixel traces of the oracle-matching kernel, copied to the host
+        (numpy, capi.TRACE_DTYPE, y*W + x): the input of debug_report."""
+        import numpy as np
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        rgb = torch.empty(width * height * 3, device=dev)
+        tr = torch.empty(width * height * np.dtype(capi.TRACE_DTYPE).itemsize, dtype=torch.uint8, device=dev)
+        self.render_trace(cam, width, height, rgb, None, None, tr)
+        torch.cuda.current_stream().synchronize()
+        return np.frombuffer(tr.cpu().numpy().tobytes(), dtype=np.dtype(capi.TRACE_DTYPE))
 
     def render_fast(self, cam, width: int, height: int, rgb, alpha=None, depth=None, precision: int = 0,
                     stream=None, timed: bool = False) -> Optional[float]:

@@ -244,7 +244,7 @@ def run_ours(args, rank: int, world: int):
     for (cam, w, h), off in zip(cams, offs):
         if not (forms & F.FORM_EXACT):
             break
-        tr = torch.zeros(w * h * 48, dtype=torch.uint8, device=dev)
+        tr = torch.zeros(w * h * np.dtype(pkg.capi.TRACE_DTYPE).itemsize, dtype=torch.uint8, device=dev)
         tmp = torch.zeros(w * h * 3, device=dev)
         scene.render_trace(cam, w, h, tmp, None, None, tr)
         torch.cuda.synchronize(dev)

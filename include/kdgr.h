@@ -301,6 +301,8 @@ typedef struct {
   uint32_t n_hit;      /* accepted hits the compositing loop reached */
   uint32_t n_blend;    /* hits composited */
   uint32_t n_restart;  /* restarts from the root after the short stack ran dry */
+  uint32_t n_found;    /* hits accepted in all visited leaves (hits_found, :1604) */
+  uint32_t max_sort;   /* most hits accepted in one leaf (max_sort_size, :1605) */
   uint64_t h_leaf;     /* visited leaf node indices, in visit order */
   uint64_t h_hit;      /* Gaussian IDs of reached hits, in compositing order */
   uint64_t h_blend;    /* Gaussian IDs of composited hits, in order */
@@ -310,6 +312,30 @@ typedef struct {
  * row order, not flipped).  Asynchronous on `stream`. */
 int kdgr_render_trace(kdgr_scene_t scene, const kdgr_camera* cam, int width, int height, float* d_rgb,
                       float* d_alpha, float* d_depth, kdgr_ray_trace* d_trace, void* stream);
+
+/* ------------------------------------------------------------ debug report
+ * Headless form of the reference's HIT_AND_NODE_COUNT_DEBUG report
+ * (cudaRenderer.cu:3173-3400).  Counters, in this order: node visits, leaf
+ * visits, intersection tests, hits found, blend ops, max sort size
+ * (kdgr_ray_trace n_inner, n_leaf, n_cand, n_found, n_blend, max_sort).
+ * Averages and totals are over pixels with at least one blend, accumulated
+ * in FP32 in pixel order as the reference does; maxima over all pixels. */
+typedef struct {
+  float avg[6];
+  float total[6];
+  int32_t max[6];
+  uint32_t n_pixels; /* pixels that blended at least one Gaussian */
+} kdgr_debug_stats;
+
+/* Reduce host-resident traces (d_trace of kdgr_render_trace copied back,
+ * y*W + x order) to `out` (nullable) and, when out_dir is non-null, write the
+ * reference's report files there: renderStats.txt, render_stats.csv,
+ * heatmap_{node_visits,leaf_visits,intersection,hits_found,blend_ops,
+ * max_sort_size}.{png,csv}, isectCnt_kd.bin and blendCnt_kd.bin.  Heatmaps
+ * use the Turbo colormap over [0, heat_max] (the reference fixes 120).  Host
+ * only; needs no GPU. */
+int kdgr_debug_report(const kdgr_ray_trace* trace, int width, int height, const char* out_dir, float heat_max,
+                      kdgr_debug_stats* out);
 
 #ifdef __cplusplus
 }

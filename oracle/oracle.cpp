@@ -7,6 +7,7 @@
 // SGRTx2Lib/cuda_math.h:260-420, e.g. dot = a.x*b.x + a.y*b.y + a.z*b.z).
 // The template parameter R is float for the oracle-matching build and
 // double for the FP64 twin.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -212,7 +213,7 @@ void trace_ray(const orc_scene* S, const Ray<R>& ray, V3<R>& C, R& A, R& D, kdgr
   C = mk<R>(0, 0, 0);
   A = 0;
   D = 0;
-  uint32_t n_inner = 0, n_leaf = 0, n_cand = 0, n_hit = 0, n_blend = 0, n_restart = 0;
+  uint32_t n_inner = 0, n_leaf = 0, n_cand = 0, n_hit = 0, n_blend = 0, n_restart = 0, n_found = 0, max_sort = 0;
   Fnv hl, hh, hb;
   R tmin = R(1e-2f), tmax = R(FLT_MAX);
   const R bmin[3] = {S->aabb[0], S->aabb[1], S->aabb[2]};
@@ -268,6 +269,9 @@ void trace_ray(const orc_scene* S, const Ray<R>& ray, V3<R>& C, R& A, R& D, kdgr
         R t;
         if (intersect<R>(ray, S->gauss + (size_t)gid * 64, t_near, t_far, &t)) hits.push_back({t, gid});
       }
+      // HIT_AND_NODE_COUNT_DEBUG counters (cudaRenderer.cu:1602-1606)
+      n_found += (uint32_t)hits.size();
+      max_sort = std::max(max_sort, (uint32_t)hits.size());
       // stable insertion sort by t (sortHits)
       for (size_t i = 1; i < hits.size(); ++i) {
         Hit<R> key = hits[i];
@@ -313,6 +317,8 @@ void trace_ray(const orc_scene* S, const Ray<R>& ray, V3<R>& C, R& A, R& D, kdgr
     tr->n_hit = n_hit;
     tr->n_blend = n_blend;
     tr->n_restart = n_restart;
+    tr->n_found = n_found;
+    tr->max_sort = max_sort;
     tr->h_leaf = hl.h;
     tr->h_hit = hh.h;
     tr->h_blend = hb.h;

@@ -16,7 +16,7 @@ REPO = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 
 TRACE_DTYPE = np.dtype([("n_inner", "<u4"), ("n_leaf", "<u4"), ("n_cand", "<u4"), ("n_hit", "<u4"),
-                        ("n_blend", "<u4"), ("n_restart", "<u4"), ("h_leaf", "<u8"), ("h_hit", "<u8"),
+                        ("n_blend", "<u4"), ("n_restart", "<u4"), ("n_found", "<u4"), ("max_sort", "<u4"), ("h_leaf", "<u8"), ("h_hit", "<u8"),
                         ("h_blend", "<u8")])
 
 

@@ -3,7 +3,7 @@ buffers and through the CPU oracle, in the same image layout."""
 import numpy as np
 import torch
 
-TRACE_BYTES = 48
+TRACE_BYTES = 56
 
 
 def gpu_exact(pkg, dev, tree, rec, cam, W, H, scales_inverted=False):
