@@ -42,6 +42,10 @@ class Tree(ctypes.Structure):
                 ("valid", ctypes.POINTER(ctypes.c_uint8)), ("n_gaussians", ctypes.c_uint32)]
 
 
+class Gaussians(ctypes.Structure):
+    _fields_ = [("records", ctypes.POINTER(ctypes.c_float)), ("n", ctypes.c_uint32)]
+
+
 class BuildStats(ctypes.Structure):
     _fields_ = [("proxy_s", ctypes.c_double), ("build_s", ctypes.c_double), ("n_triangles", ctypes.c_uint64),
                 ("n_valid", ctypes.c_uint32)]
@@ -83,6 +87,11 @@ def _declare(L: ctypes.CDLL) -> None:
     L.kdgr_write_kdt.argtypes = [ctypes.POINTER(Tree), ctypes.c_char_p]
     L.kdgr_validate_tree.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.c_uint32]
     L.kdgr_tree_free.argtypes = [ctypes.POINTER(Tree)]
+    L.kdgr_read_kdt_ascii.argtypes = [ctypes.c_char_p, ctypes.POINTER(Tree)]
+    L.kdgr_write_kdt_ascii.argtypes = [ctypes.POINTER(Tree), ctypes.c_char_p]
+    L.kdgr_read_ply.argtypes = [ctypes.c_char_p, ctypes.POINTER(Gaussians)]
+    L.kdgr_gaussians_free.argtypes = [ctypes.POINTER(Gaussians)]
+    L.kdgr_gaussians_free.restype = None
     L.kdgr_tree_free.restype = None
     for name, args in _EXTRA_SIGS.items():
         fn = getattr(L, name, None)

@@ -39,6 +39,8 @@ bool proxy_icosahedron(const float* g, float out[20][3][3]);
 // .kdt v1 binary (Kd-treeConverter.cpp:297-342, 444-495)
 int write_kdt(const HostTree& t, const char* path, std::string& err);
 int read_kdt(const char* path, HostTree& t, std::string& err);
+int write_kdt_ascii(const HostTree& t, const char* path, std::string& err);
+int read_kdt_ascii(const char* path, HostTree& t, std::string& err);
 // Structural validation: child indices in range, leaf ranges inside the
 // ID array, IDs below n_gaussians, every node reachable at most once.
 int validate_tree(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,

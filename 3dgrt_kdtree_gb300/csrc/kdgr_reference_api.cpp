@@ -113,13 +113,10 @@ void cleanupCudaResources() {
 
 int read_kd_tree_from_file(CompositeObject* object, const char* filename, int dump_format) {
   if (!object || !filename) return 0;
-  if (dump_format != KD_TREE_DUMP_IN_BINARY) {
-    fprintf(stderr, "read_kd_tree_from_file: only the binary .kdt format is supported\n");
-    return 0;
-  }
   std::lock_guard<std::mutex> lk(g_mu);
   kdgr_tree t;
-  if (kdgr_read_kdt(filename, &t) != KDGR_OK) {
+  const bool binary = dump_format == KD_TREE_DUMP_IN_BINARY;
+  if ((binary ? kdgr_read_kdt(filename, &t) : kdgr_read_kdt_ascii(filename, &t)) != KDGR_OK) {
     fprintf(stderr, "%s kd-tree File Load Error! (%s)\n", filename, kdgr_last_error());
     return 0;
   }
@@ -131,14 +128,30 @@ int read_kd_tree_from_file(CompositeObject* object, const char* filename, int du
   kt.tree_node_count = (int)g_tree.n_nodes;
   kt.prim_offset_list = g_tree.offsets;
   kt.prim_offset_count = (int)g_tree.n_offsets;
-  // .kdt header order (xmin, ymin, zmin, xmax, ymax, zmax) -> AABB[XMIN..ZMAX]
-  object->AABB[0] = g_tree.aabb[0];
-  object->AABB[2] = g_tree.aabb[1];
-  object->AABB[4] = g_tree.aabb[2];
-  object->AABB[1] = g_tree.aabb[3];
-  object->AABB[3] = g_tree.aabb[4];
-  object->AABB[5] = g_tree.aabb[5];
+  if (binary) {
+    // .kdt header order (xmin, ymin, zmin, xmax, ymax, zmax) -> AABB[XMIN..ZMAX]
+    object->AABB[0] = g_tree.aabb[0];
+    object->AABB[2] = g_tree.aabb[1];
+    object->AABB[4] = g_tree.aabb[2];
+    object->AABB[1] = g_tree.aabb[3];
+    object->AABB[3] = g_tree.aabb[4];
+    object->AABB[5] = g_tree.aabb[5];
+  }
   memcpy(kt.AABB, object->AABB, sizeof(kt.AABB));
   object->kd_tree = &kt;
   return 1;
+}
+
+bool loadGaussiansFromPly(const char* filename, std::vector<Gaussian>& gaussians) {
+  static_assert(sizeof(Gaussian) == 64 * sizeof(float), "Gaussian must be the reference's 64-float record");
+  kdgr_gaussians g;
+  if (!filename || kdgr_read_ply(filename, &g) != KDGR_OK) {
+    fprintf(stderr, "Error: Cannot load PLY file %s (%s)\n", filename ? filename : "(null)", kdgr_last_error());
+    return false;
+  }
+  gaussians.resize(g.n);
+  memcpy(gaussians.data(), g.records, sizeof(Gaussian) * (size_t)g.n);
+  kdgr_gaussians_free(&g);
+  fprintf(stderr, "\nRobustly loaded %zu gaussians based on PLY header.\n", gaussians.size());
+  return true;
 }

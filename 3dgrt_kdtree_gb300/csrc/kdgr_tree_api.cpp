@@ -71,6 +71,100 @@ int read_kdt(const char* path, HostTree& t, std::string& err) {
   return rc;
 }
 
+// ASCII form of dump_kd_tree_for_composite_object / read_kd_tree_from_file
+// (Kd-treeConverter.cpp:345-380, 496-541): "n<count>", one line per node
+// ("<X|Y|Z>|<split %f> <child><><child+1>" or "L cnt:<n> off:<offset>"),
+// "o<count>", one Gaussian ID per line.  No scene box; splits carry six
+// decimals, so a round trip through this format moves split planes.
+int write_kdt_ascii(const HostTree& t, const char* path, std::string& err) {
+  FILE* fp = fopen(path, "w");
+  if (!fp) {
+    err = std::string("cannot open ") + path + " for writing";
+    return KDGR_ERR_IO;
+  }
+  const size_t nn = t.nodes.size() / 2;
+  bool ok = fprintf(fp, "n%d\n", (int)nn) > 0;
+  static const char kAxis[3] = {'X', 'Y', 'Z'};
+  for (size_t i = 0; i < nn && ok; ++i) {
+    const uint32_t x = t.nodes[2 * i], y = t.nodes[2 * i + 1];
+    if ((x & 7u) == 3u) {
+      ok = fprintf(fp, "L cnt:%d off:%d\n", (int)(x >> 3), (int)y) > 0;
+    } else {
+      float split;
+      memcpy(&split, &y, 4);
+      const int child = (int)(x >> 3);
+      ok = fprintf(fp, "%c|%f %d<>%d\n", kAxis[x & 3u], (double)split, child, child + 1) > 0;
+    }
+  }
+  ok = ok && fprintf(fp, "o%d\n", (int)t.offsets.size()) > 0;
+  for (size_t i = 0; i < t.offsets.size() && ok; ++i) ok = fprintf(fp, "%d\n", (int)t.offsets[i]) > 0;
+  ok = (fclose(fp) == 0) && ok;
+  if (!ok) {
+    err = std::string("short write to ") + path;
+    return KDGR_ERR_IO;
+  }
+  return KDGR_OK;
+}
+
+int read_kdt_ascii(const char* path, HostTree& t, std::string& err) {
+  FILE* fp = fopen(path, "r");
+  if (!fp) {
+    err = std::string("cannot open ") + path;
+    return KDGR_ERR_IO;
+  }
+  char line[1024];
+  auto next = [&]() { return fgets(line, sizeof line, fp) != nullptr; };
+  int rc = KDGR_OK;
+  int nn = -1, no = -1;
+  memset(t.aabb, 0, sizeof t.aabb);
+  if (!next() || line[0] != 'n' || sscanf(line + 1, "%d", &nn) != 1 || nn <= 0) {
+    err = "bad ASCII .kdt header (expected n<node count>)";
+    rc = KDGR_ERR_FORMAT;
+  }
+  if (rc == KDGR_OK) t.nodes.resize(2 * (size_t)nn);
+  for (int i = 0; rc == KDGR_OK && i < nn; ++i) {
+    int a = 0, b = 0;
+    float split = 0.f;
+    if (!next()) {
+      err = "truncated ASCII .kdt node list";
+      rc = KDGR_ERR_FORMAT;
+    } else if (line[0] == 'L') {
+      if (sscanf(line + 2, "cnt:%d off:%d", &a, &b) != 2 || a < 0 || b < 0) {
+        err = "bad leaf line " + std::to_string(i);
+        rc = KDGR_ERR_FORMAT;
+      } else {
+        t.nodes[2 * i] = ((uint32_t)a << 3) | 3u;
+        t.nodes[2 * i + 1] = (uint32_t)b;
+      }
+    } else if (line[0] >= 'X' && line[0] <= 'Z' && line[1] == '|' &&
+               sscanf(line + 2, "%f %d", &split, &a) == 2 && a > 0) {
+      uint32_t bits;
+      memcpy(&bits, &split, 4);
+      t.nodes[2 * i] = ((uint32_t)a << 3) | (uint32_t)(line[0] - 'X');
+      t.nodes[2 * i + 1] = bits;
+    } else {
+      err = "bad node line " + std::to_string(i);
+      rc = KDGR_ERR_FORMAT;
+    }
+  }
+  if (rc == KDGR_OK && (!next() || line[0] != 'o' || sscanf(line + 1, "%d", &no) != 1 || no < 0)) {
+    err = "bad ASCII .kdt offset header (expected o<count>)";
+    rc = KDGR_ERR_FORMAT;
+  }
+  if (rc == KDGR_OK) t.offsets.resize((size_t)no);
+  for (int i = 0; rc == KDGR_OK && i < no; ++i) {
+    long long id = -1;
+    if (!next() || sscanf(line, "%lld", &id) != 1 || id < 0 || id > 0xFFFFFFFFll) {
+      err = "bad Gaussian ID line " + std::to_string(i);
+      rc = KDGR_ERR_FORMAT;
+    } else {
+      t.offsets[i] = (uint32_t)id;
+    }
+  }
+  fclose(fp);
+  return rc;
+}
+
 int validate_tree(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
                   uint32_t n_gaussians, std::string& err, uint32_t* depth_out) {
   if (n_nodes == 0) {
@@ -209,6 +303,24 @@ int kdgr_build_tree(const float* gaussians, uint32_t n_gaussians, const kdgr_bui
   return fill_out(t, n_gaussians, out);
 }
 
+static int finish_read(HostTree& t, const char* who, kdgr_tree* out) {
+  std::string err;
+  uint32_t depth = 0;
+  int rc = validate_tree(t.nodes.data(), (uint32_t)(t.nodes.size() / 2), t.offsets.data(),
+                         (uint32_t)t.offsets.size(), 0xFFFFFFFFu, err, &depth);
+  if (rc != KDGR_OK) {
+    set_error(std::string(who) + ": " + err);
+    return rc;
+  }
+  t.depth = depth;
+  for (size_t i = 0; i < t.nodes.size(); i += 2)
+    if ((t.nodes[i] & 7u) == 3u) {
+      ++t.n_leaves;
+      if ((t.nodes[i] >> 3) > t.max_leaf) t.max_leaf = t.nodes[i] >> 3;
+    }
+  return fill_out(t, 0, out);
+}
+
 int kdgr_read_kdt(const char* path, kdgr_tree* out) {
   if (!path || !out) {
     set_error("kdgr_read_kdt: null argument");
@@ -221,20 +333,36 @@ int kdgr_read_kdt(const char* path, kdgr_tree* out) {
     set_error("kdgr_read_kdt: " + err);
     return rc;
   }
-  uint32_t depth = 0;
-  rc = validate_tree(t.nodes.data(), (uint32_t)(t.nodes.size() / 2), t.offsets.data(), (uint32_t)t.offsets.size(),
-                     0xFFFFFFFFu, err, &depth);
+  return finish_read(t, "kdgr_read_kdt", out);
+}
+
+int kdgr_read_kdt_ascii(const char* path, kdgr_tree* out) {
+  if (!path || !out) {
+    set_error("kdgr_read_kdt_ascii: null argument");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  HostTree t;
+  std::string err;
+  int rc = read_kdt_ascii(path, t, err);
   if (rc != KDGR_OK) {
-    set_error("kdgr_read_kdt: " + err);
+    set_error("kdgr_read_kdt_ascii: " + err);
     return rc;
   }
-  t.depth = depth;
-  for (size_t i = 0; i < t.nodes.size(); i += 2)
-    if ((t.nodes[i] & 7u) == 3u) {
-      ++t.n_leaves;
-      if ((t.nodes[i] >> 3) > t.max_leaf) t.max_leaf = t.nodes[i] >> 3;
-    }
-  return fill_out(t, 0, out);
+  return finish_read(t, "kdgr_read_kdt_ascii", out);
+}
+
+int kdgr_write_kdt_ascii(const kdgr_tree* tree, const char* path) {
+  if (!tree || !path || !tree->nodes) {
+    set_error("kdgr_write_kdt_ascii: null argument");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  HostTree t;
+  t.nodes.assign(tree->nodes, tree->nodes + 2 * (size_t)tree->n_nodes);
+  t.offsets.assign(tree->offsets, tree->offsets + tree->n_offsets);
+  std::string err;
+  int rc = write_kdt_ascii(t, path, err);
+  if (rc != KDGR_OK) set_error("kdgr_write_kdt_ascii: " + err);
+  return rc;
 }
 
 int kdgr_write_kdt(const kdgr_tree* tree, const char* path) {

@@ -59,13 +59,17 @@ def build(gaussians: np.ndarray, max_level: int = 24, force_split: int = 16, ise
     return tree
 
 
-def read_kdt(path: str) -> KdTree:
+def read_kdt(path: str, ascii: bool = False) -> KdTree:
+    """read_kd_tree_from_file (Kd-treeConverter.cpp:444-541), binary or ASCII
+    format; the ASCII format has no scene box (aabb comes back zero)."""
     t = capi.Tree()
-    capi.check(capi.lib().kdgr_read_kdt(path.encode(), ctypes.byref(t)), "kdgr_read_kdt")
+    fn = "kdgr_read_kdt_ascii" if ascii else "kdgr_read_kdt"
+    capi.check(getattr(capi.lib(), fn)(path.encode(), ctypes.byref(t)), fn)
     return _take(t)
 
 
-def write_kdt(tree: KdTree, path: str) -> None:
+def write_kdt(tree: KdTree, path: str, ascii: bool = False) -> None:
+    """dump_kd_tree_for_composite_object (Kd-treeConverter.cpp:297-380)."""
     nodes = np.ascontiguousarray(tree.nodes, dtype=np.uint32)
     offs = np.ascontiguousarray(tree.offsets, dtype=np.uint32)
     t = capi.Tree()
@@ -74,7 +78,19 @@ def write_kdt(tree: KdTree, path: str) -> None:
     t.offsets = offs.ctypes.data_as(capi.c_u32p)
     t.n_offsets = offs.shape[0]
     t.aabb[:] = [float(x) for x in tree.aabb]
-    capi.check(capi.lib().kdgr_write_kdt(ctypes.byref(t), path.encode()), "kdgr_write_kdt")
+    fn = "kdgr_write_kdt_ascii" if ascii else "kdgr_write_kdt"
+    capi.check(getattr(capi.lib(), fn)(ctypes.byref(t), path.encode()), fn)
+
+
+def read_ply(path: str) -> np.ndarray:
+    """loadGaussiansFromPly (Kd-treeConverterMain.cpp:1652-1769): activated
+    (n, 64) float32 records from a binary 3DGS .ply (kdgr_read_ply)."""
+    g = capi.Gaussians()
+    capi.check(capi.lib().kdgr_read_ply(path.encode(), ctypes.byref(g)), "kdgr_read_ply")
+    try:
+        return np.ctypeslib.as_array(g.records, shape=(g.n, 64)).copy()
+    finally:
+        capi.lib().kdgr_gaussians_free(ctypes.byref(g))
 
 
 def validate(tree: KdTree, n_gaussians: int) -> None:

@@ -35,6 +35,7 @@ from __future__ import annotations
 import math
 import struct
 from dataclasses import dataclass
+from typing import Sequence
 
 import numpy as np
 
@@ -222,3 +223,51 @@ def read_kdgs(path: str) -> np.ndarray:
             raise ValueError(f"{path}: unsupported KDGS version {ver}/{fl}")
         data = np.frombuffer(f.read(n * REC_FLOATS * 4), dtype=np.float32)
     return data.reshape(n, REC_FLOATS).copy()
+
+
+# ------------------------------------------------------------------ .ply
+PLY_FIELDS = (["x", "y", "z", "nx", "ny", "nz", "f_dc_0", "f_dc_1", "f_dc_2"]
+              + [f"f_rest_{i}" for i in range(45)]
+              + ["opacity", "scale_0", "scale_1", "scale_2", "rot_0", "rot_1", "rot_2", "rot_3"])
+
+
+def raw_gaussians(n: int, seed: int = 0) -> dict:
+    """Pre-activation Gaussian fields as a trained 3DGS capture stores them
+    (position, normal, SH, opacity logit, log-scale, raw quaternion), float32,
+    drawn like the uniform workload."""
+    rng = np.random.default_rng(seed)
+    out = {
+        "x": rng.uniform(-0.5, 0.5, n), "y": rng.uniform(-0.5, 0.5, n), "z": rng.uniform(-0.5, 0.5, n),
+        "nx": np.zeros(n), "ny": np.zeros(n), "nz": np.zeros(n),
+        "opacity": rng.normal(0.0, 1.0, n),
+    }
+    for c in range(3):
+        out[f"f_dc_{c}"] = rng.normal(0.5, 0.2, n)
+        out[f"scale_{c}"] = rng.normal(math.log(0.01), 0.5, n)
+    for i in range(45):
+        out[f"f_rest_{i}"] = rng.normal(0.0, 0.05, n)
+    for i in range(4):
+        out[f"rot_{i}"] = rng.normal(0.0, 1.0, n)
+    return {k: v.astype(np.float32) for k, v in out.items()}
+
+
+def write_ply(path: str, fields: dict, order: Sequence[str] | None = None,
+              extra: Sequence[tuple] = ()) -> None:
+    """Binary little-endian .ply with one vertex element: float properties in
+    ``order`` (default: the 3DGS layout, PLY_FIELDS) plus ``extra`` properties
+    given as (ply type, name, numpy array)."""
+    order = list(order or PLY_FIELDS)
+    n = len(fields[order[0]])
+    np_types = {"float": "<f4", "double": "<f8", "uchar": "u1", "int": "<i4", "short": "<i2"}
+    cols = [(name, "float", np.asarray(fields[name], np.float32)) for name in order]
+    cols += [(name, t, np.asarray(v).astype(np_types[t])) for t, name, v in extra]
+    dt = np.dtype([(name, np_types[t]) for name, t, _ in cols])
+    data = np.zeros(n, dt)
+    for name, _, v in cols:
+        data[name] = v
+    head = ["ply", "format binary_little_endian 1.0", f"element vertex {n}"]
+    head += [f"property {t} {name}" for name, t, _ in cols]
+    head += ["end_header"]
+    with open(path, "wb") as f:
+        f.write(("\n".join(head) + "\n").encode("ascii"))
+        f.write(data.tobytes())

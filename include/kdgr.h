@@ -108,6 +108,28 @@ int kdgr_read_kdt(const char* path, kdgr_tree* out);
  * (Kd-treeConverter.cpp:297-342). */
 int kdgr_write_kdt(const kdgr_tree* tree, const char* path);
 
+/* The ASCII forms of the same two calls (KD_TREE_DUMP_IN_ASCII,
+ * Kd-treeConverter.cpp:345-380, 496-541).  The format has no scene box (aabb
+ * reads back as zeros: pass the box to kdgr_scene_create yourself) and prints
+ * splits with six decimals, so a round trip moves split planes, as in the
+ * reference. */
+int kdgr_read_kdt_ascii(const char* path, kdgr_tree* out);
+int kdgr_write_kdt_ascii(const kdgr_tree* tree, const char* path);
+
+/* Gaussians in the reference's 64-float record (Kd-treeConverter.h:319-335),
+ * activated; malloc'd by the library: kdgr_gaussians_free. */
+typedef struct {
+  float* records;
+  uint32_t n;
+} kdgr_gaussians;
+
+/* loadGaussiansFromPly (Kd-treeConverterMain.cpp:1652-1769): a binary
+ * little-endian 3DGS .ply, fields found by property name, activated (sigmoid
+ * opacity, exp scale, normalised quaternion, k_scale).  Scales come back
+ * activated, not inverted. */
+int kdgr_read_ply(const char* path, kdgr_gaussians* out);
+void kdgr_gaussians_free(kdgr_gaussians* g);
+
 /* Child/leaf ranges in bounds, IDs < n_gaussians, no node reached twice. */
 int kdgr_validate_tree(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
                        uint32_t n_gaussians);

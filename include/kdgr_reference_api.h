@@ -85,9 +85,14 @@ float renderGaussianWithCudaFrame(const Camera& camera, int width, int height, f
 void warmUp(float* d_framebuffer, cudaStream_t stream);
 /* cleanupCudaResources (KC/cudaRenderer.cu:3486-3521). */
 void cleanupCudaResources();
-/* read_kd_tree_from_file (KC/Kd-treeConverter.cpp:444-572), binary format;
- * validates the tree.  Returns 1 on success, 0 otherwise.  The arrays are
- * owned by the library until the next call or cleanupCudaResources. */
+/* read_kd_tree_from_file (KC/Kd-treeConverter.cpp:444-572), binary or ASCII
+ * format (the ASCII format has no box: object->AABB is left as it was, as in
+ * the reference); validates the tree.  Returns 1 on success, 0 otherwise.
+ * The arrays are owned by the library until the next call or
+ * cleanupCudaResources. */
 int read_kd_tree_from_file(CompositeObject* object, const char* filename, int dump_format);
+/* loadGaussiansFromPly (KC/Kd-treeConverterMain.cpp:1652-1769): a binary
+ * little-endian 3DGS .ply into activated Gaussians (kdgr_read_ply). */
+bool loadGaussiansFromPly(const char* filename, std::vector<Gaussian>& gaussians);
 
 #endif /* KDGR_REFERENCE_API_H_ */

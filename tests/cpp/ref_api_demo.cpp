@@ -3,7 +3,9 @@
 // and :3548): read the .kdt, invert the scales as the reference caller does,
 // set up, render one frame into a device framebuffer, write it to a file.
 //
-// usage: ref_api_demo scene.kdgs tree.kdt W H px py pz ux uy uz vx vy vz nx ny nz fovy aspect near out.bin
+// A scene given as .ply goes through loadGaussiansFromPly.
+//
+// usage: ref_api_demo scene.(kdgs|ply) tree.kdt W H px py pz ux uy uz vx vy vz nx ny nz fovy aspect near out.bin
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -34,7 +36,9 @@ int main(int argc, char** argv) {
     return 2;
   }
   std::vector<Gaussian> gaussians;
-  if (!read_kdgs(argv[1], gaussians)) return 3;
+  const size_t len = strlen(argv[1]);
+  const bool ply = len > 4 && strcmp(argv[1] + len - 4, ".ply") == 0;
+  if (!(ply ? loadGaussiansFromPly(argv[1], gaussians) : read_kdgs(argv[1], gaussians))) return 3;
   CompositeObject obj;
   memset(&obj, 0, sizeof(obj));
   if (!read_kd_tree_from_file(&obj, argv[2], KD_TREE_DUMP_IN_BINARY)) return 4;

@@ -20,8 +20,7 @@ def _cuda_home():
     return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
 
 
-@pytest.mark.parametrize("name", ["dense800", "cluster2k"])
-def test_reference_call_sequence_bit_exact(pkg, O, cuda, fixtures, tmp_path, name):
+def _demo(pkg, tmp_path):
     cuda_home = _cuda_home()
     exe = tmp_path / "ref_api_demo"
     libdir = os.path.dirname(pkg.capi.LIB_PATH)
@@ -30,6 +29,17 @@ def test_reference_call_sequence_bit_exact(pkg, O, cuda, fixtures, tmp_path, nam
                     "-L" + libdir, "-l:libkdgr.so", "-Wl,-rpath," + libdir,
                     "-L" + os.path.join(cuda_home, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(cuda_home, "lib64"),
                     "-o", str(exe)], check=True)
+    return exe
+
+
+def _cam_args(cam, w, h):
+    return [str(w), str(h)] + [repr(float(v)) for v in list(cam.pos) + list(cam.uaxis) + list(cam.vaxis) +
+                               list(cam.naxis)] + [repr(cam.fovy), repr(cam.aspect), repr(cam.near_c)]
+
+
+@pytest.mark.parametrize("name", ["dense800", "cluster2k"])
+def test_reference_call_sequence_bit_exact(pkg, O, cuda, fixtures, tmp_path, name):
+    exe = _demo(pkg, tmp_path)
     fx = fixtures[name]
     kdgs = tmp_path / "scene.kdgs"
     pkg.scenes.write_kdgs(str(kdgs), fx.rec)
@@ -43,6 +53,31 @@ def test_reference_call_sequence_bit_exact(pkg, O, cuda, fixtures, tmp_path, nam
     assert r.returncode == 0, r.stdout + r.stderr
     fb = np.fromfile(out, dtype=np.float32).reshape(h, w, 3)
     S = O.OracleScene(fx.tree.nodes, fx.tree.offsets, fx.tree.aabb, O.invert_scales(fx.rec))
+    rgb, _, _, _ = O.render(S, cam, w, h)
+    np.testing.assert_array_equal(fb, O.to_image(rgb, w, h))
+    assert fb.any()
+
+
+def test_reference_call_sequence_from_ply(pkg, O, cuda, tmp_path):
+    """loadGaussiansFromPly -> read_kd_tree_from_file -> setup -> frame, with
+    the oracle fed by the restatement of the reference's PLY loader."""
+    import sys
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import ply_ref
+    exe = _demo(pkg, tmp_path)
+    ply = tmp_path / "scene.ply"
+    pkg.scenes.write_ply(str(ply), pkg.scenes.raw_gaussians(3000, seed=11))
+    rec = ply_ref.load_gaussians_from_ply(str(ply))
+    tree = pkg.kdtree.build(rec)
+    kdt = tmp_path / "scene.kdt"
+    pkg.kdtree.write_kdt(tree, str(kdt))
+    cam, w, h = pkg.scenes.front_camera(64, 48), 64, 48
+    out = tmp_path / "fb.bin"
+    r = subprocess.run([str(exe), str(ply), str(kdt)] + _cam_args(cam, w, h) + [str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    fb = np.fromfile(out, dtype=np.float32).reshape(h, w, 3)
+    S = O.OracleScene(tree.nodes, tree.offsets, tree.aabb, O.invert_scales(rec))
     rgb, _, _, _ = O.render(S, cam, w, h)
     np.testing.assert_array_equal(fb, O.to_image(rgb, w, h))
     assert fb.any()
