@@ -31,7 +31,7 @@ CU_UNITS = {
     "kdgr_noalloc.cu": [],
 }
 CPP_UNITS = ["kdbuild.cpp", "kdgr_tree_api.cpp", "kdgr_api.cpp", "kdgr_batch_api.cpp", "kdgr_reference_api.cpp",
-             "kdgr_server.cpp", "kdgr_debug.cpp", "kdgr_ingest.cpp"]
+             "kdgr_server.cpp", "kdgr_debug.cpp", "kdgr_ingest.cpp", "kdgr_hybrid.cpp"]
 
 
 def _cuda_home() -> str:

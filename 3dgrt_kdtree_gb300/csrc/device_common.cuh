@@ -101,6 +101,22 @@ enum : uint32_t {
 constexpr uint32_t kMaxRaySteps = 1u << 22;
 
 // Launch entry points (render_exact.cu).
+// Secondary primitives of the hybrid kernel, device arrays:
+//   spheres: 10 floats each (center xyz, radius, material word, reflectivity,
+//            ior, color rgb); the material word is an int stored bitwise;
+//   tris:    9 floats each (three vertices), one material for all of them
+//            (tri_material: the 6 material floats, device pointer).
+struct HybridView {
+  const float* spheres;
+  const float* tris;
+  const float* tri_material;
+  int n_spheres;
+  uint32_t n_tris;
+};
+
+cudaError_t launch_hybrid(const ExactView& s, const CamInfo& cam, int width, int height, const HybridView& m,
+                          float* rgb, uint32_t* status, cudaStream_t stream);
+
 cudaError_t launch_exact(const ExactView& s, const CamInfo& cam, int width, int height, float* rgb, float* alpha,
                          float* depth, kdgr_ray_trace* trace, uint32_t* status, int kbuf, cudaStream_t stream);
 

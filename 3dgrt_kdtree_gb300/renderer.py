@@ -59,6 +59,17 @@ class DebugStats(ctypes.Structure):
                 ("n_pixels", ctypes.c_uint32)]
 
 
+class Material(ctypes.Structure):
+    _fields_ = [("material", ctypes.c_int32), ("reflectivity", ctypes.c_float), ("ior", ctypes.c_float),
+                ("color", ctypes.c_float * 3)]
+
+
+class Sphere(ctypes.Structure):
+    _fields_ = [("center", ctypes.c_float * 3), ("radius", ctypes.c_float), ("material", Material)]
+
+
+OPAQUE, MIRROR, GLASS = 0, 1, 2
+
 DEBUG_COUNTERS = ("node_visits", "leaf_visits", "intersection_tests", "hits_found", "blend_ops", "max_sort_size")
 
 
@@ -111,6 +122,16 @@ capi._EXTRA_SIGS.update({
                           ctypes.POINTER(vp)],
     "kdgr_batch_run": [vp, vp],
     "kdgr_batch_destroy": [vp],
+    "kdgr_demo_spheres": [ctypes.POINTER(Sphere)],
+    "kdgr_secondary_mesh_material_default": [ctypes.POINTER(Material)],
+    "kdgr_read_obj": [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(ctypes.c_float)),
+                      ctypes.POINTER(ctypes.c_uint32)],
+    "kdgr_free": [vp],
+    "kdgr_secondary_create": [ctypes.POINTER(Sphere), ctypes.c_int, vp, ctypes.c_uint32, ctypes.POINTER(Material),
+                              ctypes.POINTER(vp)],
+    "kdgr_secondary_destroy": [vp],
+    "kdgr_render_hybrid": [vp, ctypes.POINTER(capi.Camera), ctypes.c_int, ctypes.c_int, vp, vp, vp,
+                           ctypes.POINTER(ctypes.c_float)],
     "kdgr_debug_report": [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_float,
                           ctypes.POINTER(DebugStats)],
     "kdgr_autotune": [vp, ctypes.POINTER(View), ctypes.c_int, ctypes.c_int, vp, ctypes.POINTER(BatchConfig),
@@ -135,6 +156,66 @@ def _stream(stream) -> Optional[int]:
 
 def init(device: int = 0) -> None:
     capi.check(capi.lib().kdgr_init(device), "kdgr_init")
+
+
+def material(kind: int, reflectivity: float = 1.0, ior: float = 1.0, color=(1.0, 1.0, 1.0)) -> Material:
+    return Material(kind, reflectivity, ior, (ctypes.c_float * 3)(*color))
+
+
+def sphere(center, radius: float, mat: Material) -> Sphere:
+    return Sphere((ctypes.c_float * 3)(*center), radius, mat)
+
+
+def demo_spheres() -> list:
+    """The reference's two demo spheres: glass at (0,1,0), mirror at (0.8,1,1.2)."""
+    arr = (Sphere * 2)()
+    capi.check(capi.lib().kdgr_demo_spheres(arr), "kdgr_demo_spheres")
+    return list(arr)
+
+
+def mesh_material_default() -> Material:
+    m = Material()
+    capi.lib().kdgr_secondary_mesh_material_default(ctypes.byref(m))
+    return m
+
+
+def read_obj(path: str):
+    """loadSecondaryMesh: (n, 9) float32 triangles, axes mapped (x, -z, y)."""
+    import numpy as np
+    p = ctypes.POINTER(ctypes.c_float)()
+    n = ctypes.c_uint32()
+    capi.check(capi.lib().kdgr_read_obj(path.encode(), ctypes.byref(p), ctypes.byref(n)), "kdgr_read_obj")
+    try:
+        return np.ctypeslib.as_array(p, shape=(n.value, 9)).copy()
+    finally:
+        capi.lib().kdgr_free(p)
+
+
+class Secondary:
+    """Secondary primitives on the device (kdgr_secondary_create)."""
+
+    def __init__(self, spheres=(), tris=None, tri_material: Optional[Material] = None):
+        import numpy as np
+        arr = (Sphere * max(1, len(spheres)))(*spheres)
+        self._tris = np.ascontiguousarray(tris if tris is not None else np.zeros((0, 9)), np.float32)
+        m = tri_material if tri_material is not None else mesh_material_default()
+        h = ctypes.c_void_p()
+        capi.check(capi.lib().kdgr_secondary_create(arr, len(spheres),
+                                                    self._tris.ctypes.data if self._tris.shape[0] else None,
+                                                    self._tris.shape[0], ctypes.byref(m), ctypes.byref(h)),
+                   "kdgr_secondary_create")
+        self.handle = h.value
+
+    def close(self):
+        if self.handle:
+            capi.lib().kdgr_secondary_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def debug_report(trace, width: int, height: int, out_dir: Optional[str] = None,
@@ -215,6 +296,15 @@ class Scene:
         capi.check(capi.lib().kdgr_render_trace(self.handle, ctypes.byref(c), width, height, _ptr(rgb),
                                                 _ptr(alpha), _ptr(depth), _ptr(trace), _stream(stream)),
                    "kdgr_render_trace")
+
+    def render_hybrid(self, cam, width: int, height: int, secondary: "Secondary", rgb, stream=None) -> float:
+        """Secondary-ray kernel (kdgr_render_hybrid); returns kernel ms."""
+        c = capi.Camera.from_scene_camera(cam)
+        ms = ctypes.c_float()
+        capi.check(capi.lib().kdgr_render_hybrid(self.handle, ctypes.byref(c), width, height, secondary.handle,
+                                                 _ptr(rgb), _stream(stream), ctypes.byref(ms)),
+                   "kdgr_render_hybrid")
+        return ms.value
 
     def debug_counters(self, cam, width: int, height: int):
         """Per-pixel traces of the oracle-matching kernel, copied to the host

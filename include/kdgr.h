@@ -335,6 +335,47 @@ typedef struct {
 int kdgr_render_trace(kdgr_scene_t scene, const kdgr_camera* cam, int width, int height, float* d_rgb,
                       float* d_alpha, float* d_depth, kdgr_ray_trace* d_trace, void* stream);
 
+/* ------------------------------------------------------------ secondary rays
+ * The reference's SECONDARY_RAY renderer (renderKernelGaussian_Mesh_Hybrid,
+ * cudaRenderer.cu:2217-2311): up to five bounces; per bounce the closest
+ * secondary primitive clips the Gaussian pass (max_t), then a mirror
+ * reflects, glass refracts (or totally reflects) and an opaque surface ends
+ * the ray.  Oracle-matching arithmetic, like kdgr_render.  Output: RGB, rows
+ * flipped, each channel clamped to <= 1. */
+typedef struct {
+  int32_t material;  /* 0 opaque, 1 mirror, 2 glass */
+  float reflectivity;
+  float ior;
+  float color[3];
+} kdgr_material;
+
+typedef struct {
+  float center[3];
+  float radius;
+  kdgr_material material;
+} kdgr_sphere;
+
+typedef struct kdgr_secondary_s* kdgr_secondary_t;
+
+/* The reference's two demo spheres (cudaRenderer.cu:2158-2168). */
+int kdgr_demo_spheres(kdgr_sphere out[2]);
+/* SecondaryMesh defaults with the caller's mirror material
+ * (cudaRenderer.h:12-19, Kd-treeConverterMain.cpp:3054). */
+void kdgr_secondary_mesh_material_default(kdgr_material* m);
+/* loadSecondaryMesh (Kd-treeConverterMain.cpp:179-221): triangles of an
+ * .obj file (polygons fan-triangulated), each vertex mapped (x, y, z) ->
+ * (x, -z, y); *verts holds 9 floats per triangle, free with kdgr_free. */
+int kdgr_read_obj(const char* path, float** verts, uint32_t* n_tris);
+void kdgr_free(void* p);
+/* Upload secondary primitives: spheres, and/or one triangle mesh with one
+ * material (the reference uses one kind at a time; with both, the closest
+ * hit of either wins). */
+int kdgr_secondary_create(const kdgr_sphere* spheres, int n_spheres, const float* tri_verts, uint32_t n_tris,
+                          const kdgr_material* tri_material, kdgr_secondary_t* out);
+int kdgr_secondary_destroy(kdgr_secondary_t sec);
+int kdgr_render_hybrid(kdgr_scene_t scene, const kdgr_camera* cam, int width, int height, kdgr_secondary_t sec,
+                       float* d_rgb, void* stream, float* ms_out);
+
 /* ------------------------------------------------------------ debug report
  * Headless form of the reference's HIT_AND_NODE_COUNT_DEBUG report
  * (cudaRenderer.cu:3173-3400).  Counters, in this order: node visits, leaf

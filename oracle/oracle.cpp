@@ -207,12 +207,12 @@ inline bool composite(const Ray<R>& ray, const float* g, R t, V3<R>& C, R& A, R&
 // singlePassIntersectGaussian_sortNode_onlyShortStack, ELLIPSOID_BY_TRI
 // branch (cudaRenderer.cu:1488-1709) with BoundsRayIntersect (:379-399),
 // the 12-entry ring stack (:184-210) and the stable sortHits (:415-426).
+// The accumulators C, A, D are the caller's and are not reset (the
+// secondary-ray kernel keeps them across bounces, cudaRenderer.cu:2233-2255);
+// max_t clips the scene interval (SECONDARY_RAY, :1537-1538).
 template <typename R>
-void trace_ray(const orc_scene* S, const Ray<R>& ray, V3<R>& C, R& A, R& D, kdgr_ray_trace* tr,
-               std::vector<Hit<R>>& hits) {
-  C = mk<R>(0, 0, 0);
-  A = 0;
-  D = 0;
+void trace_core(const orc_scene* S, const Ray<R>& ray, R max_t, V3<R>& C, R& A, R& D, kdgr_ray_trace* tr,
+                std::vector<Hit<R>>& hits) {
   uint32_t n_inner = 0, n_leaf = 0, n_cand = 0, n_hit = 0, n_blend = 0, n_restart = 0, n_found = 0, max_sort = 0;
   Fnv hl, hh, hb;
   R tmin = R(1e-2f), tmax = R(FLT_MAX);
@@ -226,7 +226,8 @@ void trace_ray(const orc_scene* S, const Ray<R>& ray, V3<R>& C, R& A, R& D, kdgr
     tmin = std::fmax(std::fmin(l1, l2), tmin);
     tmax = std::fmin(std::fmax(l1, l2), tmax);
   }
-  if ((tmax >= tmin) & (tmax >= R(0))) {
+  if ((tmax >= tmin) & (tmax >= R(0)) & !(tmin > std::fmin(tmax, max_t))) {
+    tmax = std::fmin(tmax, max_t);
     const R t_scene_far = tmax;
     uint32_t cur = 0;
     R t_near = tmin, t_far = tmax;
@@ -325,6 +326,15 @@ void trace_ray(const orc_scene* S, const Ray<R>& ray, V3<R>& C, R& A, R& D, kdgr
   }
 }
 
+template <typename R>
+void trace_ray(const orc_scene* S, const Ray<R>& ray, V3<R>& C, R& A, R& D, kdgr_ray_trace* tr,
+               std::vector<Hit<R>>& hits) {
+  C = mk<R>(0, 0, 0);
+  A = 0;
+  D = 0;
+  trace_core<R>(S, ray, R(FLT_MAX), C, A, D, tr, hits);
+}
+
 // Ray generation of renderKernelGaussian_sortNode (cudaRenderer.cu:2336-2339).
 template <typename R>
 inline Ray<R> gen_ray(const orc_caminfo* c, int x, int y) {
@@ -376,9 +386,162 @@ int render(const orc_scene* s, const orc_caminfo* c, int width, int height, cons
   return KDGR_OK;
 }
 
+// ---------------------------------------------------------------- secondary
+// renderKernelGaussian_Mesh_Hybrid (cudaRenderer.cu:2217-2311) with
+// intersectSphere (:2170-2214), intersectTriangleMesh (:2111-2147) and
+// rayTriIntersect (:2085-2109); EPSILON = 1e-5f (DefineConst.h:24).
+struct SecHit {
+  bool hit = false, front = false;
+  float t = 1e8f;
+  V3<float> n{0, 0, 0}, p{0, 0, 0};
+  int mat = 0;
+  float refl = 0, ior = 0;
+  V3<float> color{0, 0, 0};
+};
+
+void sec_material(SecHit& h, const float* m) {
+  memcpy(&h.mat, &m[0], 4);
+  h.refl = m[1];
+  h.ior = m[2];
+  h.color = mk<float>(m[3], m[4], m[5]);
+}
+
+void sec_normal(SecHit& h, V3<float> d, V3<float> n) {
+  if (dot(d, n) > 0.0f) {
+    h.n = muls(n, -1.0f);
+    h.front = false;
+  } else {
+    h.n = n;
+    h.front = true;
+  }
+}
+
+SecHit intersect_secondary(const float* sph, int n_sph, const float* tri, uint32_t n_tri, const float* tri_mat,
+                           V3<float> o, V3<float> d) {
+  const float eps = 0.00001f;
+  SecHit h;
+  for (int i = 0; i < n_sph; ++i) {
+    const float* s = sph + 10 * i;
+    const V3<float> ctr = mk<float>(s[0], s[1], s[2]);
+    const V3<float> oc = sub(o, ctr);
+    const float a = dot(d, d);
+    const float b = 2.0f * dot(oc, d);
+    const float c = dot(oc, oc) - s[3] * s[3];
+    const float disc = b * b - 4.0f * a * c;
+    if (disc >= 0.0f) {
+      const float sq = std::sqrt(disc);
+      float root = (-b - sq) / (2.0f * a);
+      if (root < eps) root = (-b + sq) / (2.0f * a);
+      if (root > eps && root < h.t) {
+        h.hit = true;
+        h.t = root;
+        h.p = add(o, muls(d, root));
+        sec_normal(h, d, normalize(sub(h.p, ctr)));
+        sec_material(h, s + 4);
+      }
+    }
+  }
+  for (uint32_t i = 0; i < n_tri; ++i) {
+    const float* v = tri + 9ull * i;
+    const V3<float> v0 = mk<float>(v[0], v[1], v[2]), v1 = mk<float>(v[3], v[4], v[5]),
+                    v2 = mk<float>(v[6], v[7], v[8]);
+    const V3<float> e1 = sub(v1, v0), e2 = sub(v2, v0);
+    const V3<float> hv = cross(d, e2);
+    const float a = dot(e1, hv);
+    if (a > -eps && a < eps) continue;
+    const float f = 1.0f / a;
+    const V3<float> sv = sub(o, v0);
+    const float u = f * dot(sv, hv);
+    if (u < 0.0f || u > 1.0f) continue;
+    const V3<float> q = cross(sv, e1);
+    const float vv = f * dot(d, q);
+    if (vv < 0.0f || u + vv > 1.0f) continue;
+    const float t = f * dot(e2, q);
+    if (!(t > eps)) continue;
+    if (t < h.t) {
+      h.hit = true;
+      h.t = t;
+      h.p = add(o, muls(d, t));
+      sec_normal(h, d, normalize(cross(sub(v1, v0), sub(v2, v0))));
+      sec_material(h, tri_mat);
+    }
+  }
+  return h;
+}
+
+V3<float> hybrid_pixel(const orc_scene* S, const orc_caminfo* c, int px, int py, const float* sph, int n_sph,
+                       const float* tri, uint32_t n_tri, const float* tri_mat, std::vector<Hit<float>>& hits) {
+  Ray<float> ray = gen_ray<float>(c, px, py);
+  V3<float> fin = mk<float>(0, 0, 0), thr = mk<float>(1, 1, 1), acc = mk<float>(0, 0, 0);
+  float A = 0, D = 0;
+  for (int bounce = 0; bounce < 5; ++bounce) {
+    const SecHit h = intersect_secondary(sph, n_sph, tri, n_tri, tri_mat, ray.o, ray.d);
+    const float max_t = h.hit ? h.t : 1e8f;
+    trace_core<float>(S, ray, max_t, acc, A, D, nullptr, hits);
+    fin = add(fin, mulv(thr, acc));
+    thr = muls(thr, 1.0f - A);
+    if (thr.x < 0.01f && thr.y < 0.01f && thr.z < 0.01f) break;
+    if (!h.hit) break;
+    const V3<float> N = h.n, I = ray.d;
+    if (h.mat == 1) {
+      const V3<float> rdir = sub(I, muls(muls(N, 2.0f), dot(I, N)));
+      ray.o = add(h.p, muls(N, 1e-4f));
+      ray.d = normalize(rdir);
+      const V3<float> mc = bounce > 0 ? mk<float>(0, 0, 0) : h.color;
+      fin = add(fin, mulv(muls(thr, 1.0f - h.refl), mc));
+      thr = muls(thr, h.refl);
+    } else if (h.mat == 2) {
+      const float eta = h.front ? 1.0f / h.ior : h.ior;
+      const float cos_i = -dot(N, I);
+      const float sin_t2 = eta * eta * (1.0f - cos_i * cos_i);
+      if (sin_t2 > 1.0f) {
+        const V3<float> rdir = sub(I, muls(muls(N, 2.0f), dot(I, N)));
+        ray.o = add(h.p, muls(N, 1e-4f));
+        ray.d = normalize(rdir);
+      } else {
+        const float cos_t = std::sqrt(1.0f - sin_t2);
+        const V3<float> tdir = add(muls(I, eta), muls(N, eta * cos_i - cos_t));
+        ray.o = sub(h.p, muls(N, 1e-4f));
+        ray.d = normalize(tdir);
+      }
+      thr = mulv(thr, h.color);
+    } else {
+      fin = add(fin, mulv(thr, h.color));
+      break;
+    }
+  }
+  return mk<float>(std::fmin(fin.x, 1.0f), std::fmin(fin.y, 1.0f), std::fmin(fin.z, 1.0f));
+}
+
 }  // namespace
 
 extern "C" {
+
+int orc_render_hybrid_f32(const orc_scene* s, const orc_caminfo* c, int width, int height, const uint32_t* pix,
+                          uint32_t n_pix, const float* spheres, int n_spheres, const float* tris, uint32_t n_tris,
+                          const float* tri_material, float* rgb, int threads) {
+  if (!s || !c || !pix || !rgb || width <= 0 || height <= 0) return KDGR_ERR_INVALID_ARG;
+  int nt = threads;
+#ifdef _OPENMP
+  if (nt <= 0) nt = omp_get_max_threads();
+#else
+  nt = 1;
+#endif
+#pragma omp parallel num_threads(nt)
+  {
+    std::vector<Hit<float>> hits;
+#pragma omp for schedule(dynamic, 64)
+    for (long i = 0; i < (long)n_pix; ++i) {
+      const int px = (int)(pix[i] % (uint32_t)width), py = (int)(pix[i] / (uint32_t)width);
+      const V3<float> C = hybrid_pixel(s, c, px, py, spheres, n_spheres, tris, n_tris, tri_material, hits);
+      rgb[3 * i] = C.x;
+      rgb[3 * i + 1] = C.y;
+      rgb[3 * i + 2] = C.z;
+    }
+  }
+  return KDGR_OK;
+}
+
 
 void orc_caminfo_from_camera(const kdgr_camera* cam, int width, int height, orc_caminfo* out) {
   const float kPi = 3.14159265358979323846f;  // M_PI, cudaRenderer.h:31

@@ -61,6 +61,14 @@ int orc_render_f32(const orc_scene* s, const orc_caminfo* c, int width, int heig
 int orc_render_f64(const orc_scene* s, const orc_caminfo* c, int width, int height, const uint32_t* pix,
                    uint32_t n_pix, double* rgb, double* alpha, double* depth, kdgr_ray_trace* trace, int threads);
 
+/* The secondary-ray kernel (renderKernelGaussian_Mesh_Hybrid), FP32
+ * oracle-matching; spheres 10 floats each (center, radius, material word as
+ * int bits, reflectivity, ior, color), triangles 9 floats each with one
+ * 6-float material.  rgb per list entry, clamped to <= 1. */
+int orc_render_hybrid_f32(const orc_scene* s, const orc_caminfo* c, int width, int height, const uint32_t* pix,
+                          uint32_t n_pix, const float* spheres, int n_spheres, const float* tris, uint32_t n_tris,
+                          const float* tri_material, float* rgb, int threads);
+
 /* kdgr_expf, exported for the error test. */
 float orc_expf(float x);
 

@@ -63,6 +63,10 @@ def lib() -> ctypes.CDLL:
         for n in ("orc_render_f32", "orc_render_f64"):
             getattr(L, n).argtypes = [ctypes.POINTER(_Scene), ctypes.POINTER(CamInfo), ctypes.c_int, ctypes.c_int,
                                       vp, ctypes.c_uint32, vp, vp, vp, vp, ctypes.c_int]
+        vp = ctypes.c_void_p
+        L.orc_render_hybrid_f32.argtypes = [ctypes.POINTER(_Scene), ctypes.POINTER(CamInfo), ctypes.c_int,
+                                            ctypes.c_int, vp, ctypes.c_uint32, vp, ctypes.c_int, vp,
+                                            ctypes.c_uint32, vp, vp, ctypes.c_int]
         L.orc_expf.argtypes = [ctypes.c_float]
         L.orc_expf.restype = ctypes.c_float
         _lib = L
@@ -131,6 +135,49 @@ def render(scene: OracleScene, cam, width: int, height: int, pixels: np.ndarray 
     if rc != 0:
         raise RuntimeError(f"oracle render failed ({rc})")
     return rgb, alpha, depth, tr
+
+
+def pack_spheres(spheres) -> np.ndarray:
+    """[(center(3), radius, material, reflectivity, ior, color(3))] -> the
+    10-float layout with the material as int bits."""
+    out = np.zeros((len(spheres), 10), np.float32)
+    for i, (ctr, rad, mat, refl, ior, col) in enumerate(spheres):
+        out[i, 0:3] = ctr
+        out[i, 3] = rad
+        out[i, 4] = np.array([mat], np.int32).view(np.float32)[0]
+        out[i, 5:7] = (refl, ior)
+        out[i, 7:10] = col
+    return out
+
+
+def pack_material(mat, refl, ior, col) -> np.ndarray:
+    out = np.zeros(6, np.float32)
+    out[0] = np.array([mat], np.int32).view(np.float32)[0]
+    out[1:3] = (refl, ior)
+    out[3:6] = col
+    return out
+
+
+def render_hybrid(scene: OracleScene, cam, width: int, height: int, spheres=(), tris=None, tri_material=None,
+                  pixels: np.ndarray | None = None, threads: int = 0) -> np.ndarray:
+    """The secondary-ray kernel (FP32, oracle-matching).  spheres: list as in
+    pack_spheres; tris: (n, 9) float32; tri_material: (material, reflectivity,
+    ior, color).  Returns rgb (n, 3) in list order."""
+    if pixels is None:
+        pixels = np.arange(width * height, dtype=np.uint32)
+    pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
+    sph = pack_spheres(spheres)
+    tri = np.ascontiguousarray(tris if tris is not None else np.zeros((0, 9)), np.float32)
+    tm = pack_material(*tri_material) if tri_material is not None else np.zeros(6, np.float32)
+    rgb = np.zeros((pixels.shape[0], 3), np.float32)
+    ci = cam if isinstance(cam, CamInfo) else caminfo(cam, width, height)
+    rc = lib().orc_render_hybrid_f32(ctypes.byref(scene.s), ctypes.byref(ci), width, height, pixels.ctypes.data,
+                                     pixels.shape[0], sph.ctypes.data if len(sph) else None, len(sph),
+                                     tri.ctypes.data if tri.shape[0] else None, tri.shape[0], tm.ctypes.data,
+                                     rgb.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle hybrid render failed ({rc})")
+    return rgb
 
 
 def to_image(values: np.ndarray, width: int, height: int) -> np.ndarray:
