@@ -83,6 +83,7 @@ def _declare(L: ctypes.CDLL) -> None:
     L.kdgr_build_params_default.restype = None
     L.kdgr_build_tree.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(BuildParams), ctypes.POINTER(Tree),
                                   ctypes.POINTER(BuildStats)]
+    L.kdgr_build_tree_gpu.argtypes = L.kdgr_build_tree.argtypes
     L.kdgr_read_kdt.argtypes = [ctypes.c_char_p, ctypes.POINTER(Tree)]
     L.kdgr_write_kdt.argtypes = [ctypes.POINTER(Tree), ctypes.c_char_p]
     L.kdgr_validate_tree.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.c_uint32]

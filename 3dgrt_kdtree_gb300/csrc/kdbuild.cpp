@@ -452,15 +452,20 @@ void serialize(const Node* root, std::vector<uint32_t>& nodes, std::vector<uint3
   }
 }
 
-const float kIcoV[12][3] = {{-1.f, 1.618033988749895f, 0.f}, {1.f, 1.618033988749895f, 0.f},
-                            {0.f, 1.f, -1.618033988749895f}, {-1.618033988749895f, 0.f, -1.f},
-                            {-1.618033988749895f, 0.f, 1.f}, {0.f, 1.f, 1.618033988749895f},
-                            {1.618033988749895f, 0.f, 1.f},  {0.f, -1.f, 1.618033988749895f},
-                            {-1.f, -1.618033988749895f, 0.f}, {0.f, -1.f, -1.618033988749895f},
-                            {1.618033988749895f, 0.f, -1.f}, {1.f, -1.618033988749895f, 0.f}};
-const int kIcoF[20][3] = {{0, 1, 2},  {0, 2, 3},  {0, 3, 4},   {0, 4, 5},   {0, 5, 1},  {6, 1, 5},  {6, 5, 7},
-                          {6, 7, 11}, {6, 11, 10}, {6, 10, 1}, {8, 4, 3},   {8, 3, 9},  {8, 9, 11}, {8, 11, 7},
-                          {8, 7, 4},  {9, 3, 2},  {9, 2, 10},  {9, 10, 11}, {5, 4, 7},  {1, 10, 2}};
+}  // namespace
+
+const float kIcosaVerts[12][3] = {{-1.f, 1.618033988749895f, 0.f}, {1.f, 1.618033988749895f, 0.f},
+                                  {0.f, 1.f, -1.618033988749895f}, {-1.618033988749895f, 0.f, -1.f},
+                                  {-1.618033988749895f, 0.f, 1.f}, {0.f, 1.f, 1.618033988749895f},
+                                  {1.618033988749895f, 0.f, 1.f},  {0.f, -1.f, 1.618033988749895f},
+                                  {-1.f, -1.618033988749895f, 0.f}, {0.f, -1.f, -1.618033988749895f},
+                                  {1.618033988749895f, 0.f, -1.f}, {1.f, -1.618033988749895f, 0.f}};
+const int kIcosaFaces[20][3] = {{0, 1, 2},  {0, 2, 3},  {0, 3, 4},   {0, 4, 5},   {0, 5, 1},
+                                {6, 1, 5},  {6, 5, 7},  {6, 7, 11},  {6, 11, 10}, {6, 10, 1},
+                                {8, 4, 3},  {8, 3, 9},  {8, 9, 11},  {8, 11, 7},  {8, 7, 4},
+                                {9, 3, 2},  {9, 2, 10}, {9, 10, 11}, {5, 4, 7},   {1, 10, 2}};
+
+namespace {
 
 inline void cross3(const float* a, const float* b, float* o) {
   o[0] = ((a[1] * b[2]) - (a[2] * b[1]));
@@ -474,18 +479,25 @@ inline void cross3(const float* a, const float* b, float* o) {
 // k_iso * scale, rotated by the quaternion and moved to the mean
 // (Kd-treeConverterMain.cpp:1860-1922, 1975-2095).  Returns false when the
 // Gaussian is cut (sigma < 0.0113 or sigma < 1/255, :1990-1997).
-bool proxy_icosahedron(const float* g, float out[20][3][3]) {
+bool proxy_kiso(const float* g, float* k_iso) {
   const float sigma = g[3];
   const float kmin = 0.0113f;
   if (sigma < kmin || sigma < 1 / 255.0f) return false;
-  float k_iso = 0.0f;
-  if (sigma / kmin > 1.0f) k_iso = sqrtf(2.0f * logf(sigma / kmin)) * 0.5257311121191335703f;
+  float k = 0.0f;
+  if (sigma / kmin > 1.0f) k = sqrtf(2.0f * logf(sigma / kmin)) * 0.5257311121191335703f;
+  *k_iso = k;
+  return true;
+}
+
+bool proxy_icosahedron(const float* g, float out[20][3][3]) {
+  float k_iso;
+  if (!proxy_kiso(g, &k_iso)) return false;
   const float fs[3] = {g[4] * k_iso, g[5] * k_iso, g[6] * k_iso};
   const float* q = g + 8;
   const float qv[3] = {q[1], q[2], q[3]};
   for (int f = 0; f < 20; ++f)
     for (int l = 0; l < 3; ++l) {
-      const float* vc = kIcoV[kIcoF[f][l]];
+      const float* vc = kIcosaVerts[kIcosaFaces[f][l]];
       const float vs[3] = {vc[0] * fs[0], vc[1] * fs[1], vc[2] * fs[2]};
       float t[3], tt[3];
       cross3(qv, vs, t);

@@ -35,6 +35,14 @@ struct HostTree {
 
 int build_tree(const float* gauss, uint32_t n, const BuildParams& bp, HostTree& out, BuildStats* stats);
 bool proxy_icosahedron(const float* g, float out[20][3][3]);
+// Proxy scale k_iso of one Gaussian; false when the opacity cut drops it.
+bool proxy_kiso(const float* g, float* k_iso);
+// Unit icosahedron of the proxy mesh (Kd-treeConverterMain.cpp:1860-1922).
+extern const float kIcosaVerts[12][3];
+extern const int kIcosaFaces[20][3];
+// The same build on the current CUDA device (kdbuild_gpu.cu).
+int build_tree_gpu(const float* gauss, uint32_t n, const BuildParams& bp, HostTree& out, BuildStats* stats,
+                   std::string& err);
 
 // .kdt v1 binary (Kd-treeConverter.cpp:297-342, 444-495)
 int write_kdt(const HostTree& t, const char* path, std::string& err);

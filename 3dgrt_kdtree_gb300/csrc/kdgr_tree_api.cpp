@@ -321,6 +321,51 @@ static int finish_read(HostTree& t, const char* who, kdgr_tree* out) {
   return fill_out(t, 0, out);
 }
 
+int kdgr_build_tree_gpu(const float* gaussians, uint32_t n_gaussians, const kdgr_build_params* params,
+                        kdgr_tree* out, kdgr_build_stats* stats) {
+  if (!gaussians || n_gaussians == 0 || !out) {
+    set_error("kdgr_build_tree_gpu: null input or zero Gaussians");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  BuildParams bp;
+  if (params) {
+    bp.max_level = params->max_level;
+    bp.force_split = params->force_split;
+    bp.isect_cost = params->isect_cost;
+    bp.sah_mode = params->sah_mode;
+    bp.sort_cost = params->sort_cost;
+  }
+  if (bp.sah_mode != 0 && bp.sah_mode != 1 && bp.sah_mode != 4 && bp.sah_mode != 7) {
+    set_error("kdgr_build_tree_gpu: sah_mode must be 0, 1, 4 or 7");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (bp.max_level < 0 || bp.max_level > 60) {
+    set_error("kdgr_build_tree_gpu: max_level must be in [0, 60]");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  HostTree t;
+  BuildStats bs;
+  std::string err;
+  int rc;
+  try {
+    rc = build_tree_gpu(gaussians, n_gaussians, bp, t, &bs, err);
+  } catch (const std::bad_alloc&) {
+    set_error("kdgr_build_tree_gpu: host allocation failed");
+    return KDGR_ERR_OUT_OF_MEMORY;
+  }
+  if (rc != KDGR_OK) {
+    set_error("kdgr_build_tree_gpu: " + err);
+    return rc;
+  }
+  if (stats) {
+    stats->proxy_s = bs.proxy_s;
+    stats->build_s = bs.build_s + bs.serialize_s;
+    stats->n_triangles = bs.n_triangles;
+    stats->n_valid = bs.n_valid;
+  }
+  return fill_out(t, n_gaussians, out);
+}
+
 int kdgr_read_kdt(const char* path, kdgr_tree* out) {
   if (!path || !out) {
     set_error("kdgr_read_kdt: null argument");

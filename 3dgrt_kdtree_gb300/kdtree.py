@@ -42,8 +42,12 @@ def _take(t: capi.Tree) -> KdTree:
 
 
 def build(gaussians: np.ndarray, max_level: int = 24, force_split: int = 16, isect_cost: float = 5.0,
-          sah_mode: int = 1, sort_cost: float = 0.5, threads: int = 0) -> KdTree:
-    """Proxy mesh + SAH kd-tree over activated (non-inverted) records."""
+          sah_mode: int = 1, sort_cost: float = 0.5, threads: int = 0, device: str = "cpu") -> KdTree:
+    """Proxy mesh + SAH kd-tree over activated (non-inverted) records, on the
+    host (device="cpu", kdgr_build_tree) or on the current CUDA device
+    (device="cuda", kdgr_build_tree_gpu); both give the same tree."""
+    if device not in ("cpu", "cuda"):
+        raise ValueError("device must be 'cpu' or 'cuda'")
     L = capi.lib()
     rec = np.ascontiguousarray(gaussians, dtype=np.float32)
     if rec.ndim != 2 or rec.shape[1] != 64:
@@ -51,8 +55,9 @@ def build(gaussians: np.ndarray, max_level: int = 24, force_split: int = 16, ise
     p = capi.BuildParams(max_level, force_split, isect_cost, sah_mode, sort_cost, threads)
     t = capi.Tree()
     s = capi.BuildStats()
-    capi.check(L.kdgr_build_tree(rec.ctypes.data, rec.shape[0], ctypes.byref(p), ctypes.byref(t),
-                                 ctypes.byref(s)), "kdgr_build_tree")
+    fn = "kdgr_build_tree" if device == "cpu" else "kdgr_build_tree_gpu"
+    capi.check(getattr(L, fn)(rec.ctypes.data, rec.shape[0], ctypes.byref(p), ctypes.byref(t), ctypes.byref(s)),
+               fn)
     tree = _take(t)
     tree.stats = {"proxy_s": s.proxy_s, "build_s": s.build_s, "n_triangles": int(s.n_triangles),
                   "n_valid": int(s.n_valid)}

@@ -100,6 +100,12 @@ void kdgr_build_params_default(kdgr_build_params* params);
 int kdgr_build_tree(const float* gaussians, uint32_t n_gaussians, const kdgr_build_params* params,
                     kdgr_tree* out, kdgr_build_stats* stats);
 
+/* The same build on the current CUDA device (breadth first, one level per
+ * step, sorts and scans on the device); the tree is the one kdgr_build_tree
+ * returns, bit for bit.  Uses params->threads for nothing. */
+int kdgr_build_tree_gpu(const float* gaussians, uint32_t n_gaussians, const kdgr_build_params* params,
+                        kdgr_tree* out, kdgr_build_stats* stats);
+
 /* read_kd_tree_from_file(obj, path, KD_TREE_DUMP_IN_BINARY)
  * (Kd-treeConverter.cpp:444-495), with structural validation. */
 int kdgr_read_kdt(const char* path, kdgr_tree* out);
