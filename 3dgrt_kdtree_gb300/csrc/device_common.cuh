@@ -59,6 +59,8 @@ struct FastView {
   const uint4* sh_bf16;
   const uint32_t* aniso_idx;
   const float4* aniso;
+  const float4* leaf_test;   // test records in leaf order (FP32 form)
+  const uint4* leaf_packed;  // packed records in leaf order
   uint32_t n_nodes, n_offsets, n_gauss, top_nodes;
   float bmin[3], bmax[3];
 };

@@ -283,7 +283,8 @@ void kdgr_server_s::completer() {
 
 static uint64_t estimate_scene_bytes(uint32_t n_nodes, uint32_t n_offsets, uint32_t n, bool packed) {
   const uint64_t per = packed ? (32 + 96 + 4) : (48 + 4 + 192);
-  return 8ull * n_nodes + 4ull * n_offsets + per * n;
+  const uint64_t per_entry = 4 + (packed ? 32 : 48);  // ID + leaf-order record
+  return 8ull * n_nodes + per_entry * n_offsets + per * n;
 }
 
 extern "C" {

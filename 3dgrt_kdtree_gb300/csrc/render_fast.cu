@@ -10,13 +10,17 @@
 //     Mahalanobis distance;
 //   * hits are accepted with t* in the half-open interval [t_near, t_far),
 //     so a Gaussian straddling a split plane is composited in one leaf only;
-//   * the top levels of the tree (breadth-first, up to 2047 nodes) are
-//     staged once per CTA in shared memory; the persistent CTAs amortise it;
+//   * the tree is relaid out with its top levels breadth-first (they stay
+//     hot in L1/L2) and the rest depth-first;
 //   * the short stack (ring semantics and root restart as the reference) is
 //     in shared memory, [slot][thread];
-//   * a leaf's candidates are fetched two at a time (both ID and record loads
-//     in flight before either test), doubling the memory-level parallelism
-//     of the latency-bound candidate loop;
+//   * candidate records are stored a second time in leaf order (entry j is
+//     the record of Gaussian offsets[j]), so a leaf's candidates are one
+//     contiguous run: no ID-then-record dependent load per candidate; the
+//     ID is read only for accepted hits;
+//   * a leaf's candidates are fetched two at a time (both record loads in
+//     flight before either test), doubling the memory-level parallelism of
+//     the latency-bound candidate loop;
 //   * pixels are handed out in spatially coherent units (8x4 warp tiles or
 //     16x8 CTA blocks) so the rays sharing an SM's L1 are neighbours; the
 //     autotuner picks the schedule and the register cap (occupancy).
@@ -78,16 +82,17 @@ struct Rec {
   float4 a, b, c;
 };
 
+// Record of leaf entry `pos` (leaf-order copy).
 template <bool PACKED>
-__device__ __forceinline__ Rec load_rec(const FastView& S, uint32_t gid) {
+__device__ __forceinline__ Rec load_rec(const FastView& S, uint32_t pos) {
   Rec r;
   if (!PACKED) {
-    const float4* p = S.test + 3ull * gid;
+    const float4* p = S.leaf_test + 3ull * pos;
     r.a = __ldg(p);
     r.b = __ldg(p + 1);
     r.c = __ldg(p + 2);
   } else {
-    const uint4 u0 = __ldg(S.packed + 2ull * gid), u1 = __ldg(S.packed + 2ull * gid + 1);
+    const uint4 u0 = __ldg(S.leaf_packed + 2ull * pos), u1 = __ldg(S.leaf_packed + 2ull * pos + 1);
     r.a = make_float4(__uint_as_float(u0.x), __uint_as_float(u0.y), __uint_as_float(u0.z), __uint_as_float(u0.w));
     r.b = make_float4(__uint_as_float(u1.x), __uint_as_float(u1.y), __uint_as_float(u1.z), __uint_as_float(u1.w));
   }
@@ -110,7 +115,7 @@ __device__ __forceinline__ bool finish_test(F3 m0, F3 m1, F3 m2, F3 gro, F3 d, f
 }
 
 template <bool PACKED>
-__device__ __forceinline__ bool test_rec(const FastView& S, uint32_t gid, const Rec& r, F3 o, F3 d, float t_near,
+__device__ __forceinline__ bool test_rec(const FastView& S, uint32_t pos, const Rec& r, F3 o, F3 d, float t_near,
                                          float t_far, float* t_out, float* gray_out) {
   if (!PACKED) {
     const F3 m0 = mk(r.a.x, r.a.y, r.a.z), m1 = mk(r.b.x, r.b.y, r.b.z), m2 = mk(r.c.x, r.c.y, r.c.z);
@@ -118,7 +123,7 @@ __device__ __forceinline__ bool test_rec(const FastView& S, uint32_t gid, const 
     return finish_test(m0, m1, m2, gro, d, t_near, t_far, t_out, gray_out);
   }
   if (__float_as_uint(r.a.w) >> 31) {  // anisotropic: factors from the FP64 upload precompute
-    const float4* p = S.aniso + 3ull * __ldg(S.aniso_idx + gid);
+    const float4* p = S.aniso + 3ull * __ldg(S.aniso_idx + __ldg(S.offsets + pos));
     const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
     const F3 m0 = mk(a.x, a.y, a.z), m1 = mk(b.x, b.y, b.z), m2 = mk(c.x, c.y, c.z);
     const F3 gro = mk(dot3(m0, o) - a.w, dot3(m1, o) - b.w, dot3(m2, o) - c.w);
@@ -333,19 +338,13 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     bool overflow = false;
     for (uint32_t i = 0; i < cnt; i += 2) {
       const bool two = i + 1 < cnt;
-      const uint32_t g0 = __ldg(S.offsets + base + i);
-      const uint32_t g1 = two ? __ldg(S.offsets + base + i + 1) : g0;
-      if (g0 >= S.n_gauss || g1 >= S.n_gauss) {
-        atomicOr(status, kStatusBadId);
-        return true;
-      }
-      const Rec r0 = load_rec<PACKED>(S, g0);
-      const Rec r1 = load_rec<PACKED>(S, g1);
+      const Rec r0 = load_rec<PACKED>(S, base + i);
+      const Rec r1 = load_rec<PACKED>(S, base + (two ? i + 1 : i));
       float t, g;
-      if (test_rec<PACKED>(S, g0, r0, R.o, R.d, R.t_near, R.t_far, &t, &g) &&
+      if (test_rec<PACKED>(S, base + i, r0, R.o, R.d, R.t_near, R.t_far, &t, &g) &&
           (!have_last || t > last_t || (t == last_t && i > last_i)))
         overflow |= hb.insert(t, g, i);
-      if (two && test_rec<PACKED>(S, g1, r1, R.o, R.d, R.t_near, R.t_far, &t, &g) &&
+      if (two && test_rec<PACKED>(S, base + i + 1, r1, R.o, R.d, R.t_near, R.t_far, &t, &g) &&
           (!have_last || t > last_t || (t == last_t && i + 1 > last_i)))
         overflow |= hb.insert(t, g, i + 1);
     }
@@ -353,6 +352,10 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     for (int k = 0; k < K; ++k) {
       if (hb.t[k] == __int_as_float(0x7f800000)) break;
       const uint32_t gid = __ldg(S.offsets + base + hb.i[k]);
+      if (gid >= S.n_gauss) {
+        atomicOr(status, kStatusBadId);
+        return true;
+      }
       const float gres = __expf(-0.0555555555556f * hb.g[k] * hb.g[k]);
       const float alpha = fminf(0.99f, gauss_opacity<PACKED>(S, gid) * gres);
       if (gres < 0.0113f || alpha < 1.0f / 255.0f) continue;
@@ -733,7 +736,29 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
   }
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed upload");
   s->n_aniso = n_aniso;
+  s->d_leaf_packed = A.alloc<uint4>(2 * (size_t)(s->n_offsets ? s->n_offsets : 1));
+  if (A.err != cudaSuccess) return cuda_fail(A.err, "kdgr_scene_create: cudaMalloc (packed leaf records)");
+  e = gather_leaf_records(s->d_offsets, s->n_offsets, s->d_packed, 2, s->d_leaf_packed);
+  if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed leaf records");
   return KDGR_OK;
+}
+
+__global__ void k_gather_leaf(const uint32_t* __restrict__ offsets, uint32_t n, const uint4* __restrict__ src,
+                              int per, uint4* __restrict__ dst) {
+  const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= (size_t)n * per) return;
+  const size_t e = j / per, k = j % per;
+  dst[j] = __ldg(src + (size_t)__ldg(offsets + e) * per + k);
+}
+
+cudaError_t gather_leaf_records(const uint32_t* d_offsets, uint32_t n_offsets, const uint4* src, int per_rec,
+                                uint4* dst) {
+  if (n_offsets == 0) return cudaSuccess;
+  const size_t total = (size_t)n_offsets * per_rec;
+  k_gather_leaf<<<(unsigned)((total + 255) / 256), 256>>>(d_offsets, n_offsets, src, per_rec, dst);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return e;
 }
 
 int batch_sms() { return num_sms(); }

@@ -30,6 +30,10 @@ struct kdgr_scene_s {
   uint4* d_sh_bf16 = nullptr;
   uint32_t* d_aniso_idx = nullptr;
   float4* d_aniso = nullptr;
+  // leaf-major copies of the test records: entry j is the record of
+  // Gaussian offsets[j], so a leaf's candidates are contiguous
+  float4* d_leaf_test = nullptr;   // FP32 form, 3 x float4 per entry
+  uint4* d_leaf_packed = nullptr;  // packed form, 2 x uint4 per entry
   uint32_t n_aniso = 0;
   // per-scene status word written by kernels (error bits)
   uint32_t* d_status = nullptr;
@@ -70,6 +74,10 @@ void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std:
 // Packed precision form: BF16 SH, FP16 inverse scales / quaternion /
 // opacity, and the FP64 upload-time factors of anisotropic Gaussians.
 int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh, DevAlloc& A);
+// Gather per-Gaussian records (vec16 x per_rec each) into leaf order:
+// dst[j] = src[offsets[j]] for every entry of the ID array.
+cudaError_t gather_leaf_records(const uint32_t* d_offsets, uint32_t n_offsets, const uint4* src, int per_rec,
+                                uint4* dst);
 // Batched rendering (render_fast.cu).
 // totals: 8x4 tiles, 16x8 blocks and 32x16 super-blocks over all views.
 int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]);

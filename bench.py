@@ -145,16 +145,16 @@ def run_ours(args, rank: int, world: int):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     F.init(dev.index)
-    t0 = time.time()
     rec, cams, desc = make_workload(pkg, args.config)
-    tree = pkg.kdtree.build(rec)
+    t0 = time.time()
+    tree = pkg.kdtree.build(rec, device="cuda")  # the device builder: same tree as the host builder
     build_s = time.time() - t0
     precision = 1 if args.config == "precision" else 0
     forms = F.FORM_EXACT | (F.FORM_PACKED if precision else F.FORM_FAST)
     scene = F.Scene(tree, rec, forms=forms)
     info = scene.info()
     log(f"[bench] {desc['workload']}: tree {tree.n_nodes} nodes, {tree.offsets.size} ids, depth {tree.depth}, "
-        f"built in {build_s:.1f}s; scene {info['device_bytes'] / 1e9:.2f} GB on device")
+        f"built on the device in {build_s:.2f}s; scene {info['device_bytes'] / 1e9:.2f} GB on device")
     views, total_px, offs = F.make_views(cams)
     rays = desc["rays_per_step"]
     rgb = torch.zeros(total_px * 3, device=dev)
@@ -276,7 +276,7 @@ def run_ours(args, rank: int, world: int):
                   "plain_mrays_s": round(rays / (plain_ms * 1e-3) / 1e6, 3) if plain_ms else None,
                   "batched_over_plain": round(plain_ms / ms_step, 3) if plain_ms else None},
         "counters_per_ray": counters,
-        "tree": {"nodes": tree.n_nodes, "ids": int(tree.offsets.size), "depth": tree.depth,
+        "tree": {"nodes": tree.n_nodes, "ids": int(tree.offsets.size), "depth": tree.depth, "builder": "device",
                  "build_s": round(build_s, 2)},
         "wall_s_timed": round(wall, 3),
     }
@@ -325,7 +325,7 @@ def run_serving(args):
     t0 = time.time()
     for i, n in enumerate(sizes):
         rec = pkg.scenes.cluster_shell(n, seed=i + 1)
-        tree = pkg.kdtree.build(rec)
+        tree = pkg.kdtree.build(rec, device="cuda")
         slots.append(srv.add_scene(tree, rec))
         plain_scenes.append(F.Scene(tree, rec, forms=F.FORM_EXACT))
     log(f"[bench] serving: 4 scenes built and resident in {time.time() - t0:.1f}s, "
