@@ -53,9 +53,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     nvcc = os.path.join(cuda, "bin", "nvcc")
     inc = ["-I" + os.path.join(REPO, "include"), "-I" + CSRC]
     jobs = []
+    # KDGR_NVCC_DEFINES: extra -D options (e.g. "KDGR_FAST_HITS=2 KDGR_FAST_PIPE=1") for
+    # compile-time variants of the fast kernel
+    defs = ["-D" + d for d in os.environ.get("KDGR_NVCC_DEFINES", "").split()]
     for src, extra in CU_UNITS.items():
         obj = os.path.join(OUT_DIR, src + ".o")
-        cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *inc, *extra,
+        cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *inc, *extra, *defs,
                "-c", os.path.join(CSRC, src), "-o", obj]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")

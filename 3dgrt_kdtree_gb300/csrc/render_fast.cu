@@ -18,9 +18,9 @@
 //     the record of Gaussian offsets[j]), so a leaf's candidates are one
 //     contiguous run: no ID-then-record dependent load per candidate; the
 //     ID is read only for accepted hits;
-//   * a leaf's candidates are fetched two at a time (both record loads in
-//     flight before either test), doubling the memory-level parallelism of
-//     the latency-bound candidate loop;
+//   * a leaf's candidates are fetched kPipe at a time (all record loads in
+//     flight before the first test), multiplying the memory-level
+//     parallelism of the latency-bound candidate loop;
 //   * pixels are handed out in spatially coherent units (8x4 warp tiles or
 //     16x8 CTA blocks) so the rays sharing an SM's L1 are neighbours; the
 //     autotuner picks the schedule and the register cap (occupancy).
@@ -52,7 +52,14 @@ constexpr int kWarps = 4;
 constexpr int kThreads = kWarps * 32;
 constexpr int kTileW = 8, kTileH = 4;     // pixels per warp tile
 constexpr int kBlockW = 16, kBlockH = 8;  // pixels per CTA block (4 warps of 8x4)
-constexpr int kHits = 4;                  // hit-buffer entries per leaf pass (a leaf averages <1 hit)
+#ifndef KDGR_FAST_HITS
+#define KDGR_FAST_HITS 4
+#endif
+#ifndef KDGR_FAST_PIPE
+#define KDGR_FAST_PIPE 2
+#endif
+constexpr int kHits = KDGR_FAST_HITS;  // hit-buffer entries per leaf pass (a leaf averages <1 hit)
+constexpr int kPipe = KDGR_FAST_PIPE;  // candidate records in flight per lane
 
 struct F3 {
   float x, y, z;
@@ -336,17 +343,18 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     HitBuf<K> hb;
     hb.clear();
     bool overflow = false;
-    for (uint32_t i = 0; i < cnt; i += 2) {
-      const bool two = i + 1 < cnt;
-      const Rec r0 = load_rec<PACKED>(S, base + i);
-      const Rec r1 = load_rec<PACKED>(S, base + (two ? i + 1 : i));
-      float t, g;
-      if (test_rec<PACKED>(S, base + i, r0, R.o, R.d, R.t_near, R.t_far, &t, &g) &&
-          (!have_last || t > last_t || (t == last_t && i > last_i)))
-        overflow |= hb.insert(t, g, i);
-      if (two && test_rec<PACKED>(S, base + i + 1, r1, R.o, R.d, R.t_near, R.t_far, &t, &g) &&
-          (!have_last || t > last_t || (t == last_t && i + 1 > last_i)))
-        overflow |= hb.insert(t, g, i + 1);
+    for (uint32_t i = 0; i < cnt; i += kPipe) {
+      Rec r[kPipe];
+#pragma unroll
+      for (int k = 0; k < kPipe; ++k) r[k] = load_rec<PACKED>(S, base + min(i + k, cnt - 1));
+#pragma unroll
+      for (int k = 0; k < kPipe; ++k) {
+        float t, g;
+        const uint32_t ik = i + k;
+        if (ik < cnt && test_rec<PACKED>(S, base + ik, r[k], R.o, R.d, R.t_near, R.t_far, &t, &g) &&
+            (!have_last || t > last_t || (t == last_t && ik > last_i)))
+          overflow |= hb.insert(t, g, ik);
+      }
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -663,11 +671,12 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
     if (e != cudaSuccess) return e;
     per_sm = occ > 0 ? occ : 1;
   }
-  const uint32_t total = c.schedule == KDGR_SCHED_WARP_TILES ? total_tiles : total_blocks;
+  const bool per_warp = c.schedule == KDGR_SCHED_WARP_TILES;
+  const uint32_t total = per_warp ? total_tiles : total_blocks;
   const int chunk = c.chunk;
   uint64_t blocks = (uint64_t)num_sms() * per_sm;
   const uint64_t grabs = ((uint64_t)total + chunk - 1) / chunk;
-  const uint64_t cap = c.schedule == KDGR_SCHED_WARP_TILES ? (grabs + kWarps - 1) / kWarps : grabs;
+  const uint64_t cap = per_warp ? (grabs + kWarps - 1) / kWarps : grabs;
   if (blocks > cap) blocks = cap > 0 ? cap : 1;
   fn<<<(unsigned)blocks, kThreads, 0, st>>>(s->fast_view(), d_views, n_views, total, rgb, alpha, depth, queue,
                                             s->d_status, chunk);

@@ -82,6 +82,28 @@ def test_batch_equals_single_views_and_graph(pkg, cuda, fixtures):
     scene.close()
 
 
+def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
+    """Warp tiles and CTA blocks (with several chunk sizes and register
+    caps) only change which lane renders which pixel."""
+    fx = fixtures["cluster2k"]
+    F = pkg.renderer
+    scene = F.Scene(fx.tree, fx.rec)
+    cams = pkg.scenes.sphere_cameras(5, seed=12, resolutions=[(67, 41), (96, 64), (8, 3)])
+    views, total, _ = F.make_views(cams)
+    ref = torch.zeros(total * 3, device=cuda)
+    ref_a = torch.zeros(total, device=cuda)
+    scene.render_batch(views, len(cams), ref, ref_a)
+    for sched, chunk, minb in [(0, 1, 0), (0, 3, 8), (0, 7, 6), (1, 1, 6), (1, 2, 0), (1, 5, 8)]:
+        cfg = F.BatchConfig(sched, minb, 0, chunk, 0)
+        out = torch.full_like(ref, -1.0)
+        out_a = torch.full_like(ref_a, -1.0)
+        scene.render_batch(views, len(cams), out, out_a, cfg=cfg)
+        torch.cuda.synchronize()
+        assert float((out - ref).abs().max()) <= 1e-5, (sched, chunk, minb)
+        assert float((out_a - ref_a).abs().max()) <= 1e-5, (sched, chunk, minb)
+    scene.close()
+
+
 def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
     fx = fixtures["cluster2k"]
     F = pkg.renderer
