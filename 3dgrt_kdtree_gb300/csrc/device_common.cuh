@@ -59,7 +59,7 @@ struct FastView {
   const uint4* sh_bf16;
   const uint32_t* aniso_idx;
   const float4* aniso;
-  const float4* leaf_test;   // test records in leaf order (FP32 form)
+  const float4* leaf_pairs;  // FP32 test records in leaf order, interleaved pairs (6 x float4 per pair)
   const uint4* leaf_packed;  // packed records in leaf order
   uint32_t n_nodes, n_offsets, n_gauss, top_nodes;
   float bmin[3], bmax[3];

@@ -140,7 +140,7 @@ kdgr::FastView kdgr_scene_s::fast_view() const {
   v.sh_bf16 = d_sh_bf16;
   v.aniso_idx = d_aniso_idx;
   v.aniso = d_aniso;
-  v.leaf_test = d_leaf_test;
+  v.leaf_pairs = d_leaf_pairs;
   v.leaf_packed = d_leaf_packed;
   v.n_nodes = n_nodes;
   v.n_offsets = n_offsets;
@@ -315,10 +315,9 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
     if (cudaMemcpy(s->d_test_fast, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->d_opacity, op.data(), op.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
       return fail("kdgr_scene_create: upload (fast)");
-    s->d_leaf_test = A.alloc<float4>(3 * (size_t)(n_offsets ? n_offsets : 1));
+    s->d_leaf_pairs = A.alloc<float4>(6 * (((size_t)n_offsets + 1) / 2 + 1));
     if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (leaf records)");
-    if (gather_leaf_records(s->d_offsets, n_offsets, reinterpret_cast<const uint4*>(s->d_test_fast), 3,
-                            reinterpret_cast<uint4*>(s->d_leaf_test)) != cudaSuccess)
+    if (build_leaf_pairs(s->d_offsets, n_offsets, s->d_test_fast, s->d_leaf_pairs) != cudaSuccess)
       return fail("kdgr_scene_create: leaf records (fast)");
   }
   if (forms & KDGR_FORM_PACKED) {
@@ -338,7 +337,7 @@ int kdgr_scene_destroy(kdgr_scene_t s) {
   if (!s) return KDGR_ERR_INVALID_ARG;
   void* ps[] = {s->d_nodes,     s->d_offsets, s->d_test,      s->d_sh,          s->d_nodes_fast,
                 s->d_test_fast, s->d_opacity, s->d_packed,    s->d_sh_bf16,     s->d_aniso_idx,
-                s->d_aniso,     s->d_leaf_test, s->d_leaf_packed, s->d_status};
+                s->d_aniso,     s->d_leaf_pairs, s->d_leaf_packed, s->d_status};
   cudaError_t first = cudaSuccess;
   for (void* p : ps)
     if (p) {

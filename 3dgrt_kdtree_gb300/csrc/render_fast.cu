@@ -18,6 +18,9 @@
 //     the record of Gaussian offsets[j]), so a leaf's candidates are one
 //     contiguous run: no ID-then-record dependent load per candidate; the
 //     ID is read only for accepted hits;
+//   * FP32 form: leaf entries are stored in interleaved pairs and tested two
+//     at a time with Blackwell's packed FP32x2 instructions
+//     (fma/mul/sub.rn.f32x2), half the arithmetic instructions per test;
 //   * a leaf's candidates are fetched kPipe at a time (all record loads in
 //     flight before the first test), multiplying the memory-level
 //     parallelism of the latency-bound candidate loop;
@@ -93,8 +96,8 @@ struct Rec {
 template <bool PACKED>
 __device__ __forceinline__ Rec load_rec(const FastView& S, uint32_t pos) {
   Rec r;
-  if (!PACKED) {
-    const float4* p = S.leaf_test + 3ull * pos;
+  if (!PACKED) {  // the FP32 form reads leaf pairs (load_pair); this is its per-Gaussian record
+    const float4* p = S.test + 3ull * __ldg(S.offsets + pos);
     r.a = __ldg(p);
     r.b = __ldg(p + 1);
     r.c = __ldg(p + 2);
@@ -152,6 +155,90 @@ __device__ __forceinline__ bool test_rec(const FastView& S, uint32_t pos, const 
   const F3 q = mk(o.x - r.a.x, o.y - r.a.y, o.z - r.a.z);
   const F3 gro = mk(dot3(m0, q), dot3(m1, q), dot3(m2, q));
   return finish_test(m0, m1, m2, gro, d, t_near, t_far, t_out, gray_out);
+}
+
+// ------------------------------------------------- paired FP32x2 candidate test
+// The FP32 form stores leaf entries in pairs: pair p holds entries 2p and
+// 2p+1 interleaved, so every quantity of the test is one 64-bit register
+// with entry 2p in the low and entry 2p+1 in the high half, and one packed
+// FP32x2 instruction (fma/mul/sub.rn.f32x2) does the work of two.
+// Pair layout, 6 x 16 bytes, for rows i = 0..2 of M and b:
+//   q[2i]   = (M_i0 lo, M_i0 hi, M_i1 lo, M_i1 hi)
+//   q[2i+1] = (M_i2 lo, M_i2 hi, b_i lo, b_i hi)
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 bcast2(float x) {
+  f2 d;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(d) : "f"(x));
+  return d;
+}
+__device__ __forceinline__ void split2(f2 v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+struct PairRec {
+  ulonglong2 q[6];
+};
+
+__device__ __forceinline__ PairRec load_pair(const FastView& S, uint32_t p) {
+  const ulonglong2* a = reinterpret_cast<const ulonglong2*>(S.leaf_pairs) + 6ull * p;
+  PairRec r;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) r.q[k] = __ldg(a + k);
+  return r;
+}
+
+// The M-form test (grdu = M d, gro = M o - b, t* = -(grdu . gro) / |grdu|^2,
+// gray = |grdu x gro|^2 / |grdu|^2) for both entries of a pair.  Works with
+// ng = b - M o = -gro, so t* = (grdu . ng) / |grdu|^2 and the cross product
+// keeps its length.  Returns the pass mask (bit 0: entry 2p, bit 1: 2p+1).
+__device__ __forceinline__ unsigned test_pair(const PairRec& r, F3 o, F3 d, float t_near, float t_far, float t[2],
+                                              float g[2]) {
+  const f2 nox = bcast2(-o.x), noy = bcast2(-o.y), noz = bcast2(-o.z);
+  const f2 dx = bcast2(d.x), dy = bcast2(d.y), dz = bcast2(d.z);
+  f2 ng[3], gd[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const f2 m0 = r.q[2 * i].x, m1 = r.q[2 * i].y, m2 = r.q[2 * i + 1].x, b = r.q[2 * i + 1].y;
+    ng[i] = fma2(m0, nox, fma2(m1, noy, fma2(m2, noz, b)));
+    gd[i] = fma2(m0, dx, fma2(m1, dy, mul2(m2, dz)));
+  }
+  const f2 q = fma2(gd[0], gd[0], fma2(gd[1], gd[1], mul2(gd[2], gd[2])));
+  const f2 a = fma2(gd[0], ng[0], fma2(gd[1], ng[1], mul2(gd[2], ng[2])));
+  float q0, q1, a0, a1;
+  split2(q, q0, q1);
+  split2(a, a0, a1);
+  const float r0 = __fdividef(1.f, q0), r1 = __fdividef(1.f, q1);
+  t[0] = a0 * r0;
+  t[1] = a1 * r1;
+  unsigned m = ((t[0] >= t_near && t[0] < t_far) ? 1u : 0u) | ((t[1] >= t_near && t[1] < t_far) ? 2u : 0u);
+  if (!m) return 0u;
+  const f2 c0 = sub2(mul2(gd[1], ng[2]), mul2(gd[2], ng[1]));
+  const f2 c1 = sub2(mul2(gd[2], ng[0]), mul2(gd[0], ng[2]));
+  const f2 c2 = sub2(mul2(gd[0], ng[1]), mul2(gd[1], ng[0]));
+  const f2 cc = fma2(c0, c0, fma2(c1, c1, mul2(c2, c2)));
+  float cc0, cc1;
+  split2(cc, cc0, cc1);
+  g[0] = cc0 * r0;
+  g[1] = cc1 * r1;
+  if (!(g[0] < 8.f)) m &= ~1u;
+  if (!(g[1] < 8.f)) m &= ~2u;
+  return m;
 }
 
 template <bool PACKED>
@@ -343,17 +430,34 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     HitBuf<K> hb;
     hb.clear();
     bool overflow = false;
-    for (uint32_t i = 0; i < cnt; i += kPipe) {
-      Rec r[kPipe];
+    if constexpr (!PACKED) {
+      const uint32_t end = base + cnt;
+      for (uint32_t e = base & ~1u; e < end; e += 2) {
+        const PairRec pr = load_pair(S, e >> 1);
+        float t2[2], g2[2];
+        unsigned m = test_pair(pr, R.o, R.d, R.t_near, R.t_far, t2, g2);
+        if (e < base) m &= 2u;     // low half belongs to the previous leaf
+        if (e + 1 >= end) m &= 1u;  // high half belongs to the next leaf
 #pragma unroll
-      for (int k = 0; k < kPipe; ++k) r[k] = load_rec<PACKED>(S, base + min(i + k, cnt - 1));
+        for (int k = 0; k < 2; ++k) {
+          const uint32_t ik = e + k - base;
+          if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
+            overflow |= hb.insert(t2[k], g2[k], ik);
+        }
+      }
+    } else {
+      for (uint32_t i = 0; i < cnt; i += kPipe) {
+        Rec r[kPipe];
 #pragma unroll
-      for (int k = 0; k < kPipe; ++k) {
-        float t, g;
-        const uint32_t ik = i + k;
-        if (ik < cnt && test_rec<PACKED>(S, base + ik, r[k], R.o, R.d, R.t_near, R.t_far, &t, &g) &&
-            (!have_last || t > last_t || (t == last_t && ik > last_i)))
-          overflow |= hb.insert(t, g, ik);
+        for (int k = 0; k < kPipe; ++k) r[k] = load_rec<PACKED>(S, base + min(i + k, cnt - 1));
+#pragma unroll
+        for (int k = 0; k < kPipe; ++k) {
+          float t, g;
+          const uint32_t ik = i + k;
+          if (ik < cnt && test_rec<PACKED>(S, base + ik, r[k], R.o, R.d, R.t_near, R.t_far, &t, &g) &&
+              (!have_last || t > last_t || (t == last_t && ik > last_i)))
+            overflow |= hb.insert(t, g, ik);
+        }
       }
     }
 #pragma unroll
@@ -758,6 +862,31 @@ __global__ void k_gather_leaf(const uint32_t* __restrict__ offsets, uint32_t n, 
   if (j >= (size_t)n * per) return;
   const size_t e = j / per, k = j % per;
   dst[j] = __ldg(src + (size_t)__ldg(offsets + e) * per + k);
+}
+
+// Pair p of the FP32 leaf records: entries 2p and 2p+1 (the last entry
+// repeated when the count is odd), rows of M and b interleaved lo/hi.
+__global__ void k_build_pairs(const uint32_t* __restrict__ offsets, uint32_t n, const float4* __restrict__ test,
+                              float4* __restrict__ pairs) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= ((size_t)n + 1) / 2) return;
+  const uint32_t e0 = (uint32_t)(2 * p), e1 = min(e0 + 1, n - 1);
+  const uint32_t g0 = __ldg(offsets + e0), g1 = __ldg(offsets + e1);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float4 a = __ldg(test + 3ull * g0 + i), b = __ldg(test + 3ull * g1 + i);
+    pairs[6 * p + 2 * i] = make_float4(a.x, b.x, a.y, b.y);
+    pairs[6 * p + 2 * i + 1] = make_float4(a.z, b.z, a.w, b.w);
+  }
+}
+
+cudaError_t build_leaf_pairs(const uint32_t* d_offsets, uint32_t n_offsets, const float4* test, float4* pairs) {
+  if (n_offsets == 0) return cudaSuccess;
+  const size_t np = ((size_t)n_offsets + 1) / 2;
+  k_build_pairs<<<(unsigned)((np + 255) / 256), 256>>>(d_offsets, n_offsets, test, pairs);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return e;
 }
 
 cudaError_t gather_leaf_records(const uint32_t* d_offsets, uint32_t n_offsets, const uint4* src, int per_rec,

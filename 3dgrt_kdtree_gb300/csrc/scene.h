@@ -32,7 +32,7 @@ struct kdgr_scene_s {
   float4* d_aniso = nullptr;
   // leaf-major copies of the test records: entry j is the record of
   // Gaussian offsets[j], so a leaf's candidates are contiguous
-  float4* d_leaf_test = nullptr;   // FP32 form, 3 x float4 per entry
+  float4* d_leaf_pairs = nullptr;  // FP32 form, 6 x float4 per pair of entries
   uint4* d_leaf_packed = nullptr;  // packed form, 2 x uint4 per entry
   uint32_t n_aniso = 0;
   // per-scene status word written by kernels (error bits)
@@ -76,6 +76,7 @@ void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std:
 int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh, DevAlloc& A);
 // Gather per-Gaussian records (vec16 x per_rec each) into leaf order:
 // dst[j] = src[offsets[j]] for every entry of the ID array.
+cudaError_t build_leaf_pairs(const uint32_t* d_offsets, uint32_t n_offsets, const float4* test, float4* pairs);
 cudaError_t gather_leaf_records(const uint32_t* d_offsets, uint32_t n_offsets, const uint4* src, int per_rec,
                                 uint4* dst);
 // Batched rendering (render_fast.cu).
