@@ -10,6 +10,14 @@ A step renders one batch of views of a resident scene.  Configurations:
             256x256, 640x480, 1280x720, 1920x1080) in one persistent launch
   precision 3M Gaussians (256 clusters), 8 views at 1080p, BF16 SH and FP16
             shape arrays with FP32 arithmetic
+  serving   4 resident scenes (0.5M/1M/2M/3M), Poisson request streams at
+            --rates req/s; p50/p99 latency of the serving loop against the
+            plain per-request path
+  build     kd-tree build time of the scale scene: device builder against
+            the host builder, trees compared word for word
+Every render line carries `accuracy`: max and RMS RGB error of the batched
+frame and of the plain kernel against the FP64 oracle on a ray sample, and
+the plain kernel against the oracle-matching FP32 oracle (expected 0).
 
 `value` is the batched (persistent, CUDA-graph) form with the scene resident
 in HBM, timed with CUDA events per step with an L2 flush (a 512 MB write)
@@ -232,12 +240,17 @@ def run_ours(args, rank: int, world: int):
         for (cam, w, h), off in zip(cams, offs):
             scene.render(cam, w, h, rgb[3 * off:3 * (off + w * h)])
 
+    batched_host = host.numpy().copy()  # the last batched frame (e2e loop)
     plain_ms = None
     if not precision:
         for _ in range(max(1, args.warmup // 2)):
             plain_step()
         pm = timed_loop(plain_step, max(2, args.steps // 2))
         plain_ms = sum(pm) / len(pm)
+    else:
+        plain_step()
+    torch.cuda.synchronize(dev)
+    plain_host = rgb.cpu().numpy().copy()
 
     # counters of the oracle-matching kernel -> algorithmic bytes per step
     tr_all = []
@@ -282,6 +295,7 @@ def run_ours(args, rank: int, world: int):
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(tree, rec, cams, args.cpu_seconds)
+        out["accuracy"] = accuracy(tree, rec, cams, offs, batched_host, plain_host)
     batch.close()
     scene.close()
     return out
@@ -437,6 +451,57 @@ def cpu_sample(tree, rec, cams, seconds: float, threads: int = 0):
     return n / dt / 1e6, n, stride, nthr, dt
 
 
+def accuracy(tree, rec, cams, offs, batched, plain, n_target: int = 40000):
+    """Max and RMS RGB error of the batched frame against the FP64 oracle,
+    and of the plain kernel against the FP64 and the oracle-matching FP32
+    oracle, on a strided ray sample of every view."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    S = O.OracleScene(tree.nodes, tree.offsets, tree.aabb, O.invert_scales(rec))
+    total = sum(w * h for _, w, h in cams)
+    stride = max(1, total // n_target)
+    eb, ep, ep32 = [], [], []
+    for (cam, w, h), off in zip(cams, offs):
+        pix = np.arange(0, w * h, stride, dtype=np.uint32)
+        x, y = pix % w, pix // w
+        idx = off + (h - 1 - y).astype(np.int64) * w + x
+        r64 = O.render(S, cam, w, h, pixels=pix, precision="f64")[0]
+        r32 = O.render(S, cam, w, h, pixels=pix, precision="f32")[0]
+        eb.append(batched.reshape(-1, 3)[idx].astype(np.float64) - r64)
+        ep.append(plain.reshape(-1, 3)[idx].astype(np.float64) - r64)
+        ep32.append(plain.reshape(-1, 3)[idx] - r32)
+    eb, ep, ep32 = np.concatenate(eb), np.concatenate(ep), np.concatenate(ep32)
+    return {"vs": "FP64 oracle (CPU transcription in double)", "sampled_rays": int(eb.shape[0]),
+            "batched_max_abs": float(np.abs(eb).max()), "batched_rms": float(np.sqrt((eb ** 2).mean())),
+            "plain_max_abs": float(np.abs(ep).max()), "plain_rms": float(np.sqrt((ep ** 2).mean())),
+            "plain_vs_fp32_oracle_max_abs": float(np.abs(ep32).max())}
+
+
+def run_build(args):
+    """Tree build time on the bench scene: device builder against the host
+    builder (all host cores), trees compared word for word."""
+    pkg = importlib.import_module("3dgrt_kdtree_gb300")
+    pkg.renderer.init(0)
+    rec, _, desc = make_workload(pkg, "scale")
+    pkg.kdtree.build(pkg.scenes.uniform_cube(20_000, seed=5), device="cuda")  # context and pools warm
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.time()
+        g = pkg.kdtree.build(rec, device="cuda")
+        times.append(time.time() - t0)
+    t0 = time.time()
+    h = pkg.kdtree.build(rec)
+    host_s = time.time() - t0
+    same = bool(np.array_equal(g.nodes, h.nodes) and np.array_equal(g.offsets, h.offsets))
+    dev_s = statistics.median(times)
+    return {"metric": "kd-tree build seconds (1M cluster+shell, reference builder flags)", "value": round(dev_s, 3),
+            "unit": "s", "n_gpus": 1, "steps": len(times), "warmup": 1, "higher_is_better": False,
+            "config": {"workload": desc["workload"], "max_level": 24, "force_split": 16, "sah_mode": 1},
+            "host_builder_s": round(host_s, 2), "host_cores": os.cpu_count(), "speedup": round(host_s / dev_s, 2),
+            "identical_trees": same, "nodes": int(g.n_nodes), "ids": int(g.offsets.size), "depth": int(g.depth),
+            "triangles": int(g.stats["n_triangles"])}
+
+
 def cpu_baseline(tree, rec, cams, seconds):
     mr, n, stride, nthr, dt = cpu_sample(tree, rec, cams, seconds)
     return {"value": round(mr, 4), "unit": UNIT, "cores": nthr, "kind": "port",
@@ -474,8 +539,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="scale",
-                    choices=["scale", "small", "mid", "batching", "precision", "serving"])
-    ap.add_argument("--rates", default="25,50,100", help="serving: Poisson request rates (req/s)")
+                    choices=["scale", "small", "mid", "batching", "precision", "serving", "build"])
+    ap.add_argument("--rates", default="50,100,200,400", help="serving: Poisson request rates (req/s)")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="serving: arrivals per rate")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: default kernel config, no L2-flush buffer, no e2e/plain/CPU legs")
@@ -496,7 +561,12 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    out = run_serving(args) if args.config == "serving" else run_ours(args, rank, world)
+    if args.config == "build":
+        out = run_build(args)
+    elif args.config == "serving":
+        out = run_serving(args)
+    else:
+        out = run_ours(args, rank, world)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
