@@ -212,12 +212,9 @@ def run_ours(args, rank: int, world: int):
     if world > 1:
         torch.distributed.barrier()
     assert scene.status() == 0, "kernel raised an error status"
-    ms_step = sum(ms) / len(ms)
-    if world > 1:
-        t = torch.tensor([ms_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = rays * world / (ms_step * 1e-3) / 1e6
+    R = importlib.import_module("3dgrt_kdtree_gb300.replicas")
+    ms_step = R.max_over_ranks(sum(ms) / len(ms), dev)
+    value = R.job_throughput(rays, world, ms_step) / 1e6
 
     # e2e: cameras from the host each step, frame read back into pinned memory
     host = torch.empty(total_px * 3, dtype=torch.float32, pin_memory=True)
@@ -229,9 +226,9 @@ def run_ours(args, rank: int, world: int):
     for _ in range(args.warmup):
         e2e_step()
     ms_e2e = timed_loop(e2e_step, args.steps)
-    e2e_step_ms = sum(ms_e2e) / len(ms_e2e)
+    e2e_step_ms = R.max_over_ranks(sum(ms_e2e) / len(ms_e2e), dev)
     view_bytes = 96 * len(cams)  # ViewDesc table (96 B per view) copied host->device by kdgr_render_batch
-    e2e = {"value": rays * world / (e2e_step_ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": view_bytes,
+    e2e = {"value": R.job_throughput(rays, world, e2e_step_ms) / 1e6, "unit": UNIT, "h2d_bytes_per_step": view_bytes,
            "d2h_bytes_per_step": int(host.numel() * 4), "ms_per_step": e2e_step_ms,
            "path": "kdgr_render_batch (C ABI) + D2H of the RGB frame"}
 
