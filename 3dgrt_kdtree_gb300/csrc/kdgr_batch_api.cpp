@@ -44,12 +44,12 @@ int run_once(kdgr_scene_t s, const kdgr_batch_config& c, const std::vector<ViewD
              const uint32_t totals[3], float* rgb, float* alpha, float* depth, cudaStream_t st, const char* who) {
   const size_t vbytes = table.size() * sizeof(ViewDesc);
   void* scratch = nullptr;
-  cudaError_t e = cudaMallocAsync(&scratch, vbytes + 256, st);
+  cudaError_t e = cudaMallocAsync(&scratch, ((vbytes + 127) & ~size_t(127)) + kQueueBytes, st);
   if (e != cudaSuccess) return cuda_fail(e, who);
   ViewDesc* d_views = static_cast<ViewDesc*>(scratch);
   uint32_t* d_queue = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + ((vbytes + 127) & ~size_t(127)));
   e = cudaMemcpyAsync(d_views, table.data(), vbytes, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, kQueueBytes, st);
   if (e == cudaSuccess)
     e = launch_batch(s, c, d_views, (int)table.size(), totals, rgb, alpha, depth, d_queue, st);
   const cudaError_t ef = cudaFreeAsync(scratch, st);
@@ -139,13 +139,13 @@ int kdgr_batch_create(kdgr_scene_t s, const kdgr_view* views, int n_views, float
   for (int i = 0; i < 3; ++i) b->totals[i] = totals[i];
   cudaStream_t cap = nullptr;
   cudaError_t e = cudaMalloc(&b->d_views, table.size() * sizeof(ViewDesc));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, 4);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_queue, kQueueBytes);
   if (e == cudaSuccess)
     e = cudaMemcpy(b->d_views, table.data(), table.size() * sizeof(ViewDesc), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaError_t le = cudaMemsetAsync(b->d_queue, 0, 4, cap);
+    cudaError_t le = cudaMemsetAsync(b->d_queue, 0, kQueueBytes, cap);
     if (le == cudaSuccess)
       le = launch_batch(s, c, b->d_views, n_views, totals, rgb, alpha, depth, b->d_queue, cap);
     e = cudaStreamEndCapture(cap, &b->graph);
@@ -198,8 +198,9 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
   if (rc != KDGR_OK) return rc;
   std::vector<kdgr_batch_config> cands;
   for (int minb : {0, 6, 8})
-    for (int sched : {KDGR_SCHED_WARP_TILES, KDGR_SCHED_CTA_BLOCKS})
+    for (int sched : {KDGR_SCHED_WARP_TILES, KDGR_SCHED_CTA_BLOCKS, KDGR_SCHED_SM_STRIPS})
       for (int chunk : {1, 2}) {
+        if (sched == KDGR_SCHED_SM_STRIPS && chunk != 1) continue;  // strips take one block per claim
         kdgr_batch_config c = base;
         c.min_blocks = minb;
         c.schedule = sched;

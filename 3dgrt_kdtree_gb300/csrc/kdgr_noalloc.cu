@@ -37,7 +37,7 @@ constexpr int kNoAllocMaxViews = 256;
 constexpr size_t kTableBytes = kNoAllocMaxViews * sizeof(ViewDesc);  // 24576
 constexpr size_t kCounterOffset = (kTableBytes + 255) & ~size_t(255);
 constexpr size_t kScratchBytes = 32 * 1024;
-static_assert(kCounterOffset + sizeof(uint32_t) <= kScratchBytes, "no-alloc scratch too small");
+static_assert(kCounterOffset + kQueueBytes <= kScratchBytes, "no-alloc scratch too small");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -95,7 +95,7 @@ extern "C" int kdgr_render_batch_noalloc(kdgr_scene_t s, const kdgr_view* views,
   const cudaStream_t st = (cudaStream_t)stream;
   // pageable source: the copy is staged before the call returns
   e = cudaMemcpyAsync(d_views, table, (size_t)n_views * sizeof(ViewDesc), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, kQueueBytes, st);
   if (e == cudaSuccess) e = launch_batch(s, c, d_views, n_views, totals, rgb, alpha, depth, d_queue, st);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_render_batch_noalloc");
   return KDGR_OK;

@@ -61,6 +61,12 @@ constexpr int kBlockW = 16, kBlockH = 8;  // pixels per CTA block (4 warps of 8x
 #ifndef KDGR_FAST_PIPE
 #define KDGR_FAST_PIPE 2
 #endif
+#ifndef KDGR_FAST_PREFETCH
+#define KDGR_FAST_PREFETCH 0
+#endif
+#ifndef KDGR_FAST_STACK
+#define KDGR_FAST_STACK 12
+#endif
 constexpr int kHits = KDGR_FAST_HITS;  // hit-buffer entries per leaf pass (a leaf averages <1 hit)
 constexpr int kPipe = KDGR_FAST_PIPE;  // candidate records in flight per lane
 
@@ -340,7 +346,7 @@ struct HitBuf {
 };
 
 // ------------------------------------------------------------------ one ray
-constexpr int kStack = 16;  // short-stack ring entries (ring + root restart as the reference)
+constexpr int kStack = KDGR_FAST_STACK;  // short-stack ring entries (ring + root restart as the reference)
 
 // Per-lane ray state; one leaf is processed per call of leaf_step.
 struct Ray {
@@ -432,8 +438,16 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     bool overflow = false;
     if constexpr (!PACKED) {
       const uint32_t end = base + cnt;
+#if KDGR_FAST_PREFETCH
+      PairRec nxt = load_pair(S, (base & ~1u) >> 1);
+#endif
       for (uint32_t e = base & ~1u; e < end; e += 2) {
+#if KDGR_FAST_PREFETCH
+        const PairRec pr = nxt;
+        if (e + 2 < end) nxt = load_pair(S, (e + 2) >> 1);  // next pair in flight during this test
+#else
         const PairRec pr = load_pair(S, e >> 1);
+#endif
         float t2[2], g2[2];
         unsigned m = test_pair(pr, R.o, R.d, R.t_near, R.t_far, t2, g2);
         if (e < base) m &= 2u;     // low half belongs to the previous leaf
@@ -551,6 +565,37 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
   __shared__ float s_t[kStack][kThreads];
   __shared__ uint32_t s_work;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if constexpr (SCHED == KDGR_SCHED_SM_STRIPS) {
+    // strip of this SM: [total * k / n, total * (k + 1) / n), k = smid mod n
+    __shared__ uint32_t s_strip;
+    uint32_t smid;
+    asm("mov.u32 %0, %%smid;" : "=r"(smid));
+    const uint32_t n = (uint32_t)chunk;  // number of strips (the SM count; chunk is reused for it)
+    if (tid == 0) s_strip = smid % n;
+    uint32_t visited = 0;  // strips tried so far by this CTA (uniform)
+    while (visited < n) {
+      __syncthreads();
+      if (tid == 0) {
+        const uint32_t k = s_strip;
+        const uint32_t b0 = (uint32_t)((uint64_t)total_items * k / n), b1 = (uint32_t)((uint64_t)total_items * (k + 1) / n);
+        const uint32_t it = b0 + atomicAdd(queue + 1 + k, 1u);
+        s_work = it < b1 ? it : 0xFFFFFFFFu;
+        if (it >= b1) s_strip = (k + 1) % n;  // this strip is done: move on to the next one
+      }
+      __syncthreads();
+      const uint32_t item = s_work;
+      if (item == 0xFFFFFFFFu) {
+        ++visited;
+        continue;
+      }
+      const ViewDesc& V = views[find_view(views, n_views, item, KDGR_SCHED_CTA_BLOCKS)];
+      const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
+      const int x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
+      const int y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
+      render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
+    }
+    return;
+  }
   while (true) {
     uint32_t first;
     if constexpr (SCHED == KDGR_SCHED_CTA_BLOCKS) {
@@ -648,8 +693,9 @@ KernelFn pick_minb(int minb) {
 
 template <bool PACKED>
 KernelFn pick_sched(const kdgr_batch_config& c) {
-  return c.schedule == KDGR_SCHED_CTA_BLOCKS ? pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS>(c.min_blocks)
-                                             : pick_minb<PACKED, KDGR_SCHED_WARP_TILES>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_CTA_BLOCKS) return pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_SM_STRIPS) return pick_minb<PACKED, KDGR_SCHED_SM_STRIPS>(c.min_blocks);
+  return pick_minb<PACKED, KDGR_SCHED_WARP_TILES>(c.min_blocks);
 }
 
 KernelFn pick_kernel(const kdgr_batch_config& c) {
@@ -751,7 +797,8 @@ int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
     set_error("batch config: chunk must be in 1..64");
     return KDGR_ERR_INVALID_ARG;
   }
-  if (c.schedule != KDGR_SCHED_WARP_TILES && c.schedule != KDGR_SCHED_CTA_BLOCKS) {
+  if (c.schedule != KDGR_SCHED_WARP_TILES && c.schedule != KDGR_SCHED_CTA_BLOCKS &&
+      c.schedule != KDGR_SCHED_SM_STRIPS) {
     set_error("batch config: unknown schedule");
     return KDGR_ERR_INVALID_ARG;
   }
@@ -777,9 +824,11 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
   }
   const bool per_warp = c.schedule == KDGR_SCHED_WARP_TILES;
   const uint32_t total = per_warp ? total_tiles : total_blocks;
-  const int chunk = c.chunk;
+  // SM strips: the kernel's `chunk` argument carries the number of strips
+  const bool strips = c.schedule == KDGR_SCHED_SM_STRIPS;
+  const int chunk = strips ? std::min(num_sms(), kMaxStrips) : c.chunk;
   uint64_t blocks = (uint64_t)num_sms() * per_sm;
-  const uint64_t grabs = ((uint64_t)total + chunk - 1) / chunk;
+  const uint64_t grabs = strips ? total : ((uint64_t)total + chunk - 1) / chunk;
   const uint64_t cap = per_warp ? (grabs + kWarps - 1) / kWarps : grabs;
   if (blocks > cap) blocks = cap > 0 ? cap : 1;
   fn<<<(unsigned)blocks, kThreads, 0, st>>>(s->fast_view(), d_views, n_views, total, rgb, alpha, depth, queue,

@@ -84,6 +84,10 @@ cudaError_t gather_leaf_records(const uint32_t* d_offsets, uint32_t n_offsets, c
 int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]);
 int fill_view_table(const kdgr_view* views, int n_views, ViewDesc* out, uint32_t totals[3]);
 int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c);
+// Work-queue words of a batched launch: word 0 the global counter, words
+// 1..kMaxStrips the per-SM strip counters (zero before every launch).
+constexpr int kMaxStrips = 255;
+constexpr size_t kQueueBytes = (1 + kMaxStrips) * sizeof(uint32_t);
 cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewDesc* d_views, int n_views,
                          const uint32_t totals[3], float* rgb, float* alpha, float* depth, uint32_t* queue,
                          cudaStream_t st);

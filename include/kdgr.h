@@ -211,6 +211,9 @@ typedef struct {
 /* How the persistent kernel hands out pixels. */
 #define KDGR_SCHED_WARP_TILES 0  /* each warp takes 8x4-pixel tiles */
 #define KDGR_SCHED_CTA_BLOCKS 1  /* each CTA takes 16x8 blocks; its 4 warps render the quarters */
+#define KDGR_SCHED_SM_STRIPS 2   /* as CTA_BLOCKS, but the blocks are cut into one contiguous strip per
+                                    SM; a CTA takes the next block of its SM's strip (neighbours share
+                                    the SM's L1) and steals from the following strips when it is done */
 
 typedef struct {
   int32_t schedule;      /* KDGR_SCHED_* */

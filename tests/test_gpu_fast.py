@@ -83,8 +83,8 @@ def test_batch_equals_single_views_and_graph(pkg, cuda, fixtures):
 
 
 def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
-    """Warp tiles and CTA blocks (with several chunk sizes and register
-    caps) only change which lane renders which pixel."""
+    """Warp tiles, CTA blocks and SM strips (with several chunk sizes and
+    register caps) only change which lane renders which pixel."""
     fx = fixtures["cluster2k"]
     F = pkg.renderer
     scene = F.Scene(fx.tree, fx.rec)
@@ -93,7 +93,8 @@ def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     ref = torch.zeros(total * 3, device=cuda)
     ref_a = torch.zeros(total, device=cuda)
     scene.render_batch(views, len(cams), ref, ref_a)
-    for sched, chunk, minb in [(0, 1, 0), (0, 3, 8), (0, 7, 6), (1, 1, 6), (1, 2, 0), (1, 5, 8)]:
+    for sched, chunk, minb in [(0, 1, 0), (0, 3, 8), (0, 7, 6), (1, 1, 6), (1, 2, 0), (1, 5, 8), (2, 1, 0),
+                               (2, 1, 8)]:
         cfg = F.BatchConfig(sched, minb, 0, chunk, 0)
         out = torch.full_like(ref, -1.0)
         out_a = torch.full_like(ref_a, -1.0)
@@ -112,8 +113,8 @@ def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
     views, total, _ = F.make_views(cams)
     rgb = torch.zeros(total * 3, device=cuda)
     best, report = scene.autotune(views, len(cams), rgb)
-    assert best.schedule in (0, 1) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
-    assert len(report.strip().splitlines()) == 12
+    assert best.schedule in (0, 1, 2) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
+    assert len(report.strip().splitlines()) == 15
     ref = torch.zeros_like(rgb)
     scene.render_batch(views, len(cams), ref)
     out = torch.zeros_like(rgb)
