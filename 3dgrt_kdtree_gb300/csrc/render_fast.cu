@@ -594,35 +594,35 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
       const int y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
       render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
     }
-    return;
-  }
-  while (true) {
-    uint32_t first;
-    if constexpr (SCHED == KDGR_SCHED_CTA_BLOCKS) {
-      __syncthreads();
-      if (tid == 0) s_work = atomicAdd(queue, (uint32_t)chunk);
-      __syncthreads();
-      first = s_work;
-    } else {
-      uint32_t f = 0;
-      if (lane == 0) f = atomicAdd(queue, (uint32_t)chunk);
-      first = __shfl_sync(0xFFFFFFFFu, f, 0);
-    }
-    if (first >= total_items) break;
-    const uint32_t last = min(first + (uint32_t)chunk, total_items);
-    for (uint32_t item = first; item < last; ++item) {
-      const ViewDesc& V = views[find_view(views, n_views, item, SCHED)];
-      int x, y;
-      if (SCHED == KDGR_SCHED_CTA_BLOCKS) {
-        const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
-        x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
-        y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
+  } else {
+    while (true) {
+      uint32_t first;
+      if constexpr (SCHED == KDGR_SCHED_CTA_BLOCKS) {
+        __syncthreads();
+        if (tid == 0) s_work = atomicAdd(queue, (uint32_t)chunk);
+        __syncthreads();
+        first = s_work;
       } else {
-        const uint32_t lt = item - __ldg(&V.wt_base), nx = __ldg(&V.wt_x);
-        x = (int)(lt % nx) * kTileW + (lane & 7);
-        y = (int)(lt / nx) * kTileH + (lane >> 3);
+        uint32_t f = 0;
+        if (lane == 0) f = atomicAdd(queue, (uint32_t)chunk);
+        first = __shfl_sync(0xFFFFFFFFu, f, 0);
       }
-      render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
+      if (first >= total_items) break;
+      const uint32_t last = min(first + (uint32_t)chunk, total_items);
+      for (uint32_t item = first; item < last; ++item) {
+        const ViewDesc& V = views[find_view(views, n_views, item, SCHED)];
+        int x, y;
+        if (SCHED == KDGR_SCHED_CTA_BLOCKS) {
+          const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
+          x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
+          y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
+        } else {
+          const uint32_t lt = item - __ldg(&V.wt_base), nx = __ldg(&V.wt_x);
+          x = (int)(lt % nx) * kTileW + (lane & 7);
+          y = (int)(lt / nx) * kTileH + (lane >> 3);
+        }
+        render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
+      }
     }
   }
 }
