@@ -554,7 +554,7 @@ __device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, 
 //               its four warps render the four quarters, so the rays sharing
 //               the SM's L1 are neighbours.
 // MINB caps registers so that MINB CTAs fit per SM (0: compiler's choice).
-template <bool PACKED, int SCHED, int MINB>
+template <bool PACKED, int SCHED, int MINB, int KB>
 __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, const ViewDesc* __restrict__ views,
                                                                  int n_views, uint32_t total_items,
                                                                  float* __restrict__ rgb,
@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
       const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
       const int x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
       const int y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
-      render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
+      render_px<KB, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
     }
   } else {
     while (true) {
@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
           x = (int)(lt % nx) * kTileW + (lane & 7);
           y = (int)(lt / nx) * kTileH + (lane >> 3);
         }
-        render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
+        render_px<KB, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
       }
     }
   }
@@ -684,18 +684,23 @@ __global__ void k_aniso_fp64(const float* __restrict__ src, uint32_t n, float4* 
 using KernelFn = void (*)(FastView, const ViewDesc*, int, uint32_t, float*, float*, float*, uint32_t*, uint32_t*,
                           int);
 
-template <bool PACKED, int SCHED>
+template <bool PACKED, int SCHED, int KB>
 KernelFn pick_minb(int minb) {
-  if (minb >= 8) return k_render_batch<PACKED, SCHED, 8>;
-  if (minb >= 6) return k_render_batch<PACKED, SCHED, 6>;
-  return k_render_batch<PACKED, SCHED, 0>;
+  if (minb >= 8) return k_render_batch<PACKED, SCHED, 8, KB>;
+  if (minb >= 6) return k_render_batch<PACKED, SCHED, 6, KB>;
+  return k_render_batch<PACKED, SCHED, 0, KB>;
+}
+
+template <bool PACKED, int KB>
+KernelFn pick_sched_k(const kdgr_batch_config& c) {
+  if (c.schedule == KDGR_SCHED_CTA_BLOCKS) return pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS, KB>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_SM_STRIPS) return pick_minb<PACKED, KDGR_SCHED_SM_STRIPS, KB>(c.min_blocks);
+  return pick_minb<PACKED, KDGR_SCHED_WARP_TILES, KB>(c.min_blocks);
 }
 
 template <bool PACKED>
 KernelFn pick_sched(const kdgr_batch_config& c) {
-  if (c.schedule == KDGR_SCHED_CTA_BLOCKS) return pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS>(c.min_blocks);
-  if (c.schedule == KDGR_SCHED_SM_STRIPS) return pick_minb<PACKED, KDGR_SCHED_SM_STRIPS>(c.min_blocks);
-  return pick_minb<PACKED, KDGR_SCHED_WARP_TILES>(c.min_blocks);
+  return c.hit_buffer == 8 ? pick_sched_k<PACKED, 8>(c) : pick_sched_k<PACKED, kHits>(c);
 }
 
 KernelFn pick_kernel(const kdgr_batch_config& c) {
@@ -800,6 +805,10 @@ int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
   if (c.schedule != KDGR_SCHED_WARP_TILES && c.schedule != KDGR_SCHED_CTA_BLOCKS &&
       c.schedule != KDGR_SCHED_SM_STRIPS) {
     set_error("batch config: unknown schedule");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (c.hit_buffer != 0 && c.hit_buffer != 4 && c.hit_buffer != 8) {
+    set_error("batch config: hit_buffer must be 0, 4 or 8");
     return KDGR_ERR_INVALID_ARG;
   }
   if (c.min_blocks != 0 && c.min_blocks != 6 && c.min_blocks != 8) {

@@ -221,6 +221,8 @@ typedef struct {
   int32_t blocks_per_sm; /* persistent CTAs per SM; 0 = occupancy maximum */
   int32_t chunk;         /* work items taken per queue operation (1..64) */
   int32_t precision;     /* 0: FP32 arrays (KDGR_FORM_FAST); 1: BF16/FP16 arrays (KDGR_FORM_PACKED) */
+  int32_t hit_buffer;    /* per-leaf register hit buffer: 4 or 8 entries (0 = 4); a leaf with more
+                            accepted hits is re-scanned for the next ones */
 } kdgr_batch_config;
 
 void kdgr_batch_config_default(kdgr_batch_config* cfg);

@@ -93,9 +93,9 @@ def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     ref = torch.zeros(total * 3, device=cuda)
     ref_a = torch.zeros(total, device=cuda)
     scene.render_batch(views, len(cams), ref, ref_a)
-    for sched, chunk, minb in [(0, 1, 0), (0, 3, 8), (0, 7, 6), (1, 1, 6), (1, 2, 0), (1, 5, 8), (2, 1, 0),
-                               (2, 1, 8)]:
-        cfg = F.BatchConfig(sched, minb, 0, chunk, 0)
+    for sched, chunk, minb, kb in [(0, 1, 0, 4), (0, 3, 8, 8), (0, 7, 6, 4), (1, 1, 6, 8), (1, 2, 0, 4),
+                                   (1, 5, 8, 4), (2, 1, 0, 8), (2, 1, 8, 4)]:
+        cfg = F.BatchConfig(sched, minb, 0, chunk, 0, kb)
         out = torch.full_like(ref, -1.0)
         out_a = torch.full_like(ref_a, -1.0)
         scene.render_batch(views, len(cams), out, out_a, cfg=cfg)
@@ -114,7 +114,8 @@ def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
     rgb = torch.zeros(total * 3, device=cuda)
     best, report = scene.autotune(views, len(cams), rgb)
     assert best.schedule in (0, 1, 2) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
-    assert len(report.strip().splitlines()) == 15
+    assert len(report.strip().splitlines()) == 16
+    assert best.hit_buffer in (4, 8)
     ref = torch.zeros_like(rgb)
     scene.render_batch(views, len(cams), ref)
     out = torch.zeros_like(rgb)
