@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
 // arrays (scenes[] in device memory).  One persistent launch serves the
 // requests of all resident scenes queued in a tick.
 template <bool PACKED>
-__global__ void __launch_bounds__(kThreads, 6) k_render_multi(const FastView* __restrict__ scenes,
+__global__ void __launch_bounds__(kThreads, 8) k_render_multi(const FastView* __restrict__ scenes,
                                                               const ViewDesc* __restrict__ views, int n_views,
                                                               uint32_t total_items, float* __restrict__ rgb,
                                                               uint32_t* queue, uint32_t* status) {

@@ -15,6 +15,8 @@ A step renders one batch of views of a resident scene.  Configurations:
             plain per-request path
   build     kd-tree build time of the scale scene: device builder against
             the host builder, trees compared word for word
+  hybrid    secondary-ray renderer on the scale scene (demo spheres and a
+            mirror quad), against the plain render of the same view
 Every render line carries `accuracy`: max and RMS RGB error of the batched
 frame and of the plain kernel against the FP64 oracle on a ray sample, and
 the plain kernel against the oracle-matching FP32 oracle (expected 0).
@@ -238,14 +240,10 @@ def run_ours(args, rank: int, world: int):
             scene.render(cam, w, h, rgb[3 * off:3 * (off + w * h)])
 
     batched_host = host.numpy().copy()  # the last batched frame (e2e loop)
-    plain_ms = None
-    if not precision:
-        for _ in range(max(1, args.warmup // 2)):
-            plain_step()
-        pm = timed_loop(plain_step, max(2, args.steps // 2))
-        plain_ms = sum(pm) / len(pm)
-    else:
+    for _ in range(max(1, args.warmup // 2)):
         plain_step()
+    pm = timed_loop(plain_step, max(2, args.steps // 2))
+    plain_ms = sum(pm) / len(pm)
     torch.cuda.synchronize(dev)
     plain_host = rgb.cpu().numpy().copy()
 
@@ -499,6 +497,77 @@ def run_build(args):
             "triangles": int(g.stats["n_triangles"])}
 
 
+def run_hybrid(args):
+    """Secondary-ray renderer (the reference's SECONDARY_RAY build) on the
+    1M scene at 1080p: the reference's two demo spheres (glass, mirror) and
+    a mirror quad behind the scene; primary rays per second, the plain
+    render of the same view beside it, and a bit-exactness check of a ray
+    sample against the oracle."""
+    import torch
+    pkg = importlib.import_module("3dgrt_kdtree_gb300")
+    F = pkg.renderer
+    dev = torch.device("cuda", 0)
+    F.init(0)
+    rec, cams, desc = make_workload(pkg, "scale")
+    tree = pkg.kdtree.build(rec, device="cuda")
+    scene = F.Scene(tree, rec, forms=F.FORM_EXACT)
+    quad = np.array([[-1.6, -1.6, -1.7, 1.6, -1.6, -1.7, 1.6, 1.6, -1.7],
+                     [-1.6, -1.6, -1.7, 1.6, 1.6, -1.7, -1.6, 1.6, -1.7]], np.float32)
+    mat = F.mesh_material_default()
+    sec = F.Secondary(F.demo_spheres(), quad, mat)
+    cam, w, h = cams[0]
+    rgb = torch.zeros(w * h * 3, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, k):
+        out = []
+        for _ in range(k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            out.append(a.elapsed_time(b))
+        return sum(out) / len(out)
+
+    for _ in range(args.warmup):
+        scene.render_hybrid(cam, w, h, sec, rgb)
+    clocks = ClockSampler(0)
+    ms = timed(lambda: scene.render_hybrid(cam, w, h, sec, rgb), args.steps)
+    clk = clocks.stop()
+    torch.cuda.synchronize(dev)
+    hyb = rgb.cpu().numpy().copy()
+    for _ in range(args.warmup):
+        scene.render(cam, w, h, rgb)
+    plain_ms = timed(lambda: scene.render(cam, w, h, rgb), args.steps)
+    assert scene.status() == 0
+    out = {"metric": "Mrays/s (hybrid secondary rays, primary rays counted)", "value": round(w * h / (ms * 1e-3) / 1e6, 3),
+           "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": desc["workload"] + ", 2 demo spheres (glass, mirror) + mirror quad, <=5 bounces",
+                      "l2": "flushed between timed steps (512 MB write)"},
+           "plain_ms_per_step": round(plain_ms, 4), "hybrid_over_plain_time": round(ms / plain_ms, 3),
+           "clocks": clk, "gpu_launches": args.steps}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle as O
+        S = O.OracleScene(tree.nodes, tree.offsets, tree.aabb, O.invert_scales(rec))
+        pix = np.arange(0, w * h, 211, dtype=np.uint32)
+        sph = [(tuple(x.center), x.radius, x.material.material, x.material.reflectivity, x.material.ior,
+                tuple(x.material.color)) for x in F.demo_spheres()]
+        want = O.render_hybrid(S, cam, w, h, spheres=sph, tris=quad,
+                               tri_material=(mat.material, mat.reflectivity, mat.ior, tuple(mat.color)), pixels=pix)
+        x, y = pix % w, pix // w
+        got = hyb.reshape(-1, 3)[(h - 1 - y).astype(np.int64) * w + x]
+        out["accuracy"] = {"vs": "oracle FP32 hybrid transcription", "sampled_rays": int(pix.size),
+                           "max_abs": float(np.abs(got - want).max())}
+    sec.close()
+    scene.close()
+    return out
+
+
 def cpu_baseline(tree, rec, cams, seconds):
     mr, n, stride, nthr, dt = cpu_sample(tree, rec, cams, seconds)
     return {"value": round(mr, 4), "unit": UNIT, "cores": nthr, "kind": "port",
@@ -536,7 +605,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="scale",
-                    choices=["scale", "small", "mid", "batching", "precision", "serving", "build"])
+                    choices=["scale", "small", "mid", "batching", "precision", "serving", "build", "hybrid"])
     ap.add_argument("--rates", default="50,100,200,400", help="serving: Poisson request rates (req/s)")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="serving: arrivals per rate")
     ap.add_argument("--profile", action="store_true",
@@ -560,6 +629,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.config == "build":
         out = run_build(args)
+    elif args.config == "hybrid":
+        out = run_hybrid(args)
     elif args.config == "serving":
         out = run_serving(args)
     else:
