@@ -27,9 +27,10 @@
 //   * pixels are handed out in spatially coherent units (8x4 warp tiles or
 //     16x8 CTA blocks) so the rays sharing an SM's L1 are neighbours; the
 //     autotuner picks the schedule and the register cap (occupancy).
-//   * precision form: FP16 inverse scales / quaternion / opacity and BF16
-//     SH (32 + 96 bytes per Gaussian instead of 64 + 192); Gaussians whose
-//     scale ratio exceeds 1e3 read factors from the FP64 upload precompute.
+//   * precision form: FP16 rows of M with an FP32 mean and BF16 SH (32 + 96
+//     bytes per Gaussian instead of 48 + 192); Gaussians whose scale ratio
+//     exceeds 1e3 (or whose factors leave the FP16 range) read FP32 factors
+//     from the FP64 upload precompute.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -93,7 +94,8 @@ __device__ __forceinline__ float2 h2f(uint32_t w) {
 //           b = M mu (FP64 upload precompute).  Storing Sigma^-1 = M^T M
 //           instead would square the condition number (a scale ratio of
 //           2500 gives ~6e6, beyond FP32), so the factor is kept;
-//   packed: a = (mu, +-opacity), b = FP16 halves (1/s, quaternion).
+//   packed: a = (mu, FP16 pair (M22, flag)), b = FP16 pairs of the other
+//           eight entries of M; flag != 0 selects the FP64-precomputed table.
 struct Rec {
   float4 a, b, c;
 };
@@ -138,26 +140,19 @@ __device__ __forceinline__ bool test_rec(const FastView& S, uint32_t pos, const 
     const F3 gro = mk(dot3(m0, o) - r.a.w, dot3(m1, o) - r.b.w, dot3(m2, o) - r.c.w);
     return finish_test(m0, m1, m2, gro, d, t_near, t_far, t_out, gray_out);
   }
-  if (__float_as_uint(r.a.w) >> 31) {  // anisotropic: factors from the FP64 upload precompute
+  const float2 m22f = h2f(__float_as_uint(r.a.w));
+  if (m22f.y != 0.f) {  // flagged: factors from the FP64 upload precompute
     const float4* p = S.aniso + 3ull * __ldg(S.aniso_idx + __ldg(S.offsets + pos));
     const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
     const F3 m0 = mk(a.x, a.y, a.z), m1 = mk(b.x, b.y, b.z), m2 = mk(c.x, c.y, c.z);
     const F3 gro = mk(dot3(m0, o) - a.w, dot3(m1, o) - b.w, dot3(m2, o) - c.w);
     return finish_test(m0, m1, m2, gro, d, t_near, t_far, t_out, gray_out);
   }
-  const float2 s01 = h2f(__float_as_uint(r.b.x)), s2 = h2f(__float_as_uint(r.b.y));
-  const float2 qwx = h2f(__float_as_uint(r.b.z)), qyz = h2f(__float_as_uint(r.b.w));
-  float qr = qwx.x, x = qwx.y, y = qyz.x, z = qyz.y;
-  const float qn = rsqrtf(fmaf(qr, qr, fmaf(x, x, fmaf(y, y, z * z))));
-  qr *= qn;
-  x *= qn;
-  y *= qn;
-  z *= qn;
-  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
-  const float rx = qr * x, ry = qr * y, rz = qr * z;
-  const F3 m0 = mk(s01.x * (1.f - 2.f * (yy + zz)), s01.x * 2.f * (xy + rz), s01.x * 2.f * (xz - ry));
-  const F3 m1 = mk(s01.y * 2.f * (xy - rz), s01.y * (1.f - 2.f * (xx + zz)), s01.y * 2.f * (yz + rx));
-  const F3 m2 = mk(s2.x * 2.f * (xz + ry), s2.x * 2.f * (yz - rx), s2.x * (1.f - 2.f * (xx + yy)));
+  // FP16 rows of M, FP32 mean: gro = M (o - mu) keeps the rounding a small,
+  // consistent perturbation of the Gaussian (no M o - M mu cancellation)
+  const float2 a01 = h2f(__float_as_uint(r.b.x)), a2b0 = h2f(__float_as_uint(r.b.y));
+  const float2 b12 = h2f(__float_as_uint(r.b.z)), c01 = h2f(__float_as_uint(r.b.w));
+  const F3 m0 = mk(a01.x, a01.y, a2b0.x), m1 = mk(a2b0.y, b12.x, b12.y), m2 = mk(c01.x, c01.y, m22f.x);
   const F3 q = mk(o.x - r.a.x, o.y - r.a.y, o.z - r.a.z);
   const F3 gro = mk(dot3(m0, q), dot3(m1, q), dot3(m2, q));
   return finish_test(m0, m1, m2, gro, d, t_near, t_far, t_out, gray_out);
@@ -249,8 +244,7 @@ __device__ __forceinline__ unsigned test_pair(const PairRec& r, F3 o, F3 d, floa
 
 template <bool PACKED>
 __device__ __forceinline__ float gauss_opacity(const FastView& S, uint32_t gid) {
-  if (!PACKED) return __ldg(S.opacity + gid);
-  return fabsf(__uint_as_float(__ldg(&S.packed[2ull * gid].w)));
+  return __ldg(S.opacity + gid);
 }
 
 // eval_sh_final(3, dir, g) (cudaRenderer.cu:487-558), FMA form.
@@ -858,24 +852,40 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
     memcpy(&w, &h, 4);
     return w;
   };
+  std::vector<float> opac(n);
   for (size_t i = 0; i < n; ++i) {
     const float* r = g + 64 * i;
     const float* gs = giscl + 3 * i;
     uint32_t* p = packed.data() + 8 * i;
     const double smax = 1.0 / std::min(std::min((double)gs[0], (double)gs[1]), (double)gs[2]);
     const double smin = 1.0 / std::max(std::max((double)gs[0], (double)gs[1]), (double)gs[2]);
-    const bool aniso = smax > kAnisoRatio * smin;
-    uint32_t op_bits;
-    memcpy(&op_bits, &r[3], 4);
-    op_bits = (op_bits & 0x7FFFFFFFu) | (aniso ? 0x80000000u : 0u);  // sign bit flags the FP64 factor table
+    // M = diag(1/s) R^T in FP64 (rows), then FP16
+    const double qr = r[8], qx = r[9], qy = r[10], qz = r[11];
+    const double xx = qx * qx, yy = qy * qy, zz = qz * qz, xy = qx * qy, xz = qx * qz, yz = qy * qz;
+    const double rx = qr * qx, ry = qr * qy, rz = qr * qz;
+    const double rt[3][3] = {{1 - 2 * (yy + zz), 2 * (xy + rz), 2 * (xz - ry)},
+                             {2 * (xy - rz), 1 - 2 * (xx + zz), 2 * (yz + rx)},
+                             {2 * (xz + ry), 2 * (yz - rx), 1 - 2 * (xx + yy)}};
+    float m[3][3];
+    double mmax = 0;
+    for (int row = 0; row < 3; ++row)
+      for (int c = 0; c < 3; ++c) {
+        const double v = (double)gs[row] * rt[row][c];
+        m[row][c] = (float)v;
+        mmax = std::max(mmax, std::fabs(v));
+      }
+    // very anisotropic Gaussians, and factors beyond the FP16 range, take the
+    // FP64-precomputed FP32 factors instead
+    const bool aniso = smax > kAnisoRatio * smin || mmax > 30000.0;
     memcpy(&p[0], &r[0], 4);
     memcpy(&p[1], &r[1], 4);
     memcpy(&p[2], &r[2], 4);
-    p[3] = op_bits;
-    p[4] = pk(gs[0], gs[1]);
-    p[5] = pk(gs[2], 0.f);
-    p[6] = pk(r[8], r[9]);
-    p[7] = pk(r[10], r[11]);
+    p[3] = pk(m[2][2], aniso ? 1.f : 0.f);
+    p[4] = pk(m[0][0], m[0][1]);
+    p[5] = pk(m[0][2], m[1][0]);
+    p[6] = pk(m[1][1], m[1][2]);
+    p[7] = pk(m[2][0], m[2][1]);
+    opac[i] = r[3];
     if (aniso) {
       aidx[i] = n_aniso++;
       const float src[10] = {gs[0], gs[1], gs[2], r[8], r[9], r[10], r[11], r[0], r[1], r[2]};
@@ -885,6 +895,12 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
       __nv_bfloat16 b = __float2bfloat16_rn(sh[48 * i + k]);
       memcpy(&shb[48 * i + k], &b, 2);
     }
+  }
+  if (!s->d_opacity) {  // the FP32 form allocates it too
+    s->d_opacity = A.alloc<float>(n);
+    if (A.err == cudaSuccess &&
+        cudaMemcpy(s->d_opacity, opac.data(), n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+      return cuda_fail(cudaErrorUnknown, "kdgr_scene_create: opacity upload (packed)");
   }
   s->d_packed = A.alloc<uint4>(2 * n);
   s->d_sh_bf16 = A.alloc<uint4>(6 * n);
