@@ -89,31 +89,23 @@ __device__ __forceinline__ float2 h2f(uint32_t w) {
 }
 
 // ----------------------------------------------------------- candidate test
-// Records of one candidate as loaded from memory.
-//   FP32:   (M0, b0) (M1, b1) (M2, b2): rows of M = diag(1/s) R^T and
-//           b = M mu (FP64 upload precompute).  Storing Sigma^-1 = M^T M
-//           instead would square the condition number (a scale ratio of
-//           2500 gives ~6e6, beyond FP32), so the factor is kept;
-//   packed: a = (mu, FP16 pair (M22, flag)), b = FP16 pairs of the other
-//           eight entries of M; flag != 0 selects the FP64-precomputed table.
+// Candidate records.  FP32 form: rows of M = diag(1/s) R^T with b = M mu
+// (FP64 upload precompute), read as interleaved pairs (load_pair below).
+// Storing Sigma^-1 = M^T M instead would square the condition number (a
+// scale ratio of 2500 gives ~6e6, beyond FP32), so the factor is kept.
+// Packed form (this record): a = (mu, FP16 pair (M22, flag)), b = FP16 pairs
+// of the other eight entries of M; flag != 0 selects the FP64-precomputed
+// table.
 struct Rec {
-  float4 a, b, c;
+  float4 a, b;
 };
 
-// Record of leaf entry `pos` (leaf-order copy).
-template <bool PACKED>
+// Packed record of leaf entry `pos` (leaf-order copy).
 __device__ __forceinline__ Rec load_rec(const FastView& S, uint32_t pos) {
   Rec r;
-  if (!PACKED) {  // the FP32 form reads leaf pairs (load_pair); this is its per-Gaussian record
-    const float4* p = S.test + 3ull * __ldg(S.offsets + pos);
-    r.a = __ldg(p);
-    r.b = __ldg(p + 1);
-    r.c = __ldg(p + 2);
-  } else {
-    const uint4 u0 = __ldg(S.leaf_packed + 2ull * pos), u1 = __ldg(S.leaf_packed + 2ull * pos + 1);
-    r.a = make_float4(__uint_as_float(u0.x), __uint_as_float(u0.y), __uint_as_float(u0.z), __uint_as_float(u0.w));
-    r.b = make_float4(__uint_as_float(u1.x), __uint_as_float(u1.y), __uint_as_float(u1.z), __uint_as_float(u1.w));
-  }
+  const uint4 u0 = __ldg(S.leaf_packed + 2ull * pos), u1 = __ldg(S.leaf_packed + 2ull * pos + 1);
+  r.a = make_float4(__uint_as_float(u0.x), __uint_as_float(u0.y), __uint_as_float(u0.z), __uint_as_float(u0.w));
+  r.b = make_float4(__uint_as_float(u1.x), __uint_as_float(u1.y), __uint_as_float(u1.z), __uint_as_float(u1.w));
   return r;
 }
 
@@ -132,14 +124,9 @@ __device__ __forceinline__ bool finish_test(F3 m0, F3 m1, F3 m2, F3 gro, F3 d, f
   return gray < 8.f;
 }
 
-template <bool PACKED>
+// The test of one packed record (leaf entry `pos`).
 __device__ __forceinline__ bool test_rec(const FastView& S, uint32_t pos, const Rec& r, F3 o, F3 d, float t_near,
                                          float t_far, float* t_out, float* gray_out) {
-  if (!PACKED) {
-    const F3 m0 = mk(r.a.x, r.a.y, r.a.z), m1 = mk(r.b.x, r.b.y, r.b.z), m2 = mk(r.c.x, r.c.y, r.c.z);
-    const F3 gro = mk(dot3(m0, o) - r.a.w, dot3(m1, o) - r.b.w, dot3(m2, o) - r.c.w);
-    return finish_test(m0, m1, m2, gro, d, t_near, t_far, t_out, gray_out);
-  }
   const float2 m22f = h2f(__float_as_uint(r.a.w));
   if (m22f.y != 0.f) {  // flagged: factors from the FP64 upload precompute
     const float4* p = S.aniso + 3ull * __ldg(S.aniso_idx + __ldg(S.offsets + pos));
@@ -457,12 +444,12 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
       for (uint32_t i = 0; i < cnt; i += kPipe) {
         Rec r[kPipe];
 #pragma unroll
-        for (int k = 0; k < kPipe; ++k) r[k] = load_rec<PACKED>(S, base + min(i + k, cnt - 1));
+        for (int k = 0; k < kPipe; ++k) r[k] = load_rec(S, base + min(i + k, cnt - 1));
 #pragma unroll
         for (int k = 0; k < kPipe; ++k) {
           float t, g;
           const uint32_t ik = i + k;
-          if (ik < cnt && test_rec<PACKED>(S, base + ik, r[k], R.o, R.d, R.t_near, R.t_far, &t, &g) &&
+          if (ik < cnt && test_rec(S, base + ik, r[k], R.o, R.d, R.t_near, R.t_far, &t, &g) &&
               (!have_last || t > last_t || (t == last_t && ik > last_i)))
             overflow |= hb.insert(t, g, ik);
         }
