@@ -4,6 +4,7 @@
 // (cudaRenderer.cu:314-360).
 #include "kdgr_reference_api.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -20,6 +21,25 @@ bool g_have_tree = false;
 bool g_have_frame = false;
 kdgr_camera g_last_cam;
 int g_last_w = 0, g_last_h = 0;
+// SECONDARY_RAY build: secondary primitives (demo spheres and/or mesh)
+kdgr_secondary_t g_sec_spheres = nullptr, g_sec_mesh = nullptr;
+bool g_hybrid = false;
+int g_secondary_prim = KDGR_SECONDARY_SPHERE;
+
+void drop_secondary() {
+  if (g_sec_spheres) kdgr_secondary_destroy(g_sec_spheres);
+  if (g_sec_mesh) kdgr_secondary_destroy(g_sec_mesh);
+  g_sec_spheres = g_sec_mesh = nullptr;
+  g_hybrid = false;
+}
+
+int render_frame(const kdgr_camera& cam, int width, int height, float* fb, cudaStream_t stream, float* ms) {
+  if (g_hybrid) {
+    kdgr_secondary_t sec = g_secondary_prim == KDGR_SECONDARY_TRI ? g_sec_mesh : g_sec_spheres;
+    return kdgr_render_hybrid(g_scene, &cam, width, height, sec, fb, (void*)stream, ms);
+  }
+  return kdgr_render(g_scene, &cam, width, height, fb, nullptr, nullptr, (void*)stream, ms);
+}
 
 kdgr_camera to_camera(const Camera& c) {
   kdgr_camera k;
@@ -58,6 +78,7 @@ void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vecto
     kdgr_scene_destroy(g_scene);
     g_scene = nullptr;
   }
+  drop_secondary();
   // CompositeObject.AABB is (xmin, xmax, ymin, ymax, zmin, zmax); the scene
   // takes the .kdt order (xmin, ymin, zmin, xmax, ymax, zmax)
   const float aabb[6] = {object.AABB[0], object.AABB[2], object.AABB[4],
@@ -72,6 +93,34 @@ void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vecto
   }
 }
 
+void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vector<Gaussian>& gaussians,
+                                 SecondaryMesh& secondaryMesh) {
+  renderGaussianWithCudaSetup(object, gaussians);
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_scene) return;
+  kdgr_sphere sph[2];
+  kdgr_demo_spheres(sph);
+  int rc = kdgr_secondary_create(sph, 2, nullptr, 0, nullptr, &g_sec_spheres);
+  const uint32_t n_tris = (uint32_t)std::min<size_t>((size_t)std::max(secondaryMesh.triangleCount, 0),
+                                                     secondaryMesh.vert.size() / 3);
+  kdgr_material mat{secondaryMesh.materialType, secondaryMesh.reflectivity, secondaryMesh.ior,
+                    {secondaryMesh.color.x, secondaryMesh.color.y, secondaryMesh.color.z}};
+  if (rc == KDGR_OK)
+    rc = kdgr_secondary_create(nullptr, 0, reinterpret_cast<const float*>(secondaryMesh.vert.data()), n_tris, &mat,
+                               &g_sec_mesh);
+  if (rc != KDGR_OK) {
+    fprintf(stderr, "[CUDA Error] secondary mesh setup failed: %s\n", kdgr_last_error());
+    drop_secondary();
+    return;
+  }
+  g_hybrid = true;
+}
+
+void setSecondaryPrimitive(int prim) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_secondary_prim = prim == KDGR_SECONDARY_TRI ? KDGR_SECONDARY_TRI : KDGR_SECONDARY_SPHERE;
+}
+
 float renderGaussianWithCudaFrame(const Camera& camera, int width, int height, float* d_framebuffer,
                                   cudaStream_t stream) {
   std::lock_guard<std::mutex> lk(g_mu);
@@ -81,7 +130,7 @@ float renderGaussianWithCudaFrame(const Camera& camera, int width, int height, f
   }
   const kdgr_camera cam = to_camera(camera);
   float ms = 0.f;
-  const int rc = kdgr_render(g_scene, &cam, width, height, d_framebuffer, nullptr, nullptr, (void*)stream, &ms);
+  const int rc = render_frame(cam, width, height, d_framebuffer, stream, &ms);
   if (rc != KDGR_OK) {
     fprintf(stderr, "[CUDA Error] render failed: %s\n", kdgr_last_error());
     return 0.f;
@@ -97,13 +146,13 @@ void warmUp(float* d_framebuffer, cudaStream_t stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_scene || !g_have_frame) return;
   float ms = 0.f;
-  if (kdgr_render(g_scene, &g_last_cam, g_last_w, g_last_h, d_framebuffer, nullptr, nullptr, (void*)stream, &ms) ==
-      KDGR_OK)
+  if (render_frame(g_last_cam, g_last_w, g_last_h, d_framebuffer, stream, &ms) == KDGR_OK)
     printf("WarmUp: %f\n", ms > 0.f ? 1000.0f / ms : 0.f);
 }
 
 void cleanupCudaResources() {
   std::lock_guard<std::mutex> lk(g_mu);
+  drop_secondary();
   if (g_scene) kdgr_scene_destroy(g_scene);
   g_scene = nullptr;
   g_have_frame = false;

@@ -71,10 +71,36 @@ typedef struct _cam {
 #define KD_TREE_DUMP_IN_ASCII 0
 #define KD_TREE_DUMP_IN_BINARY 1
 
+/* SecondaryMesh of the SECONDARY_RAY build (KC/cudaRenderer.h:12-19): the
+ * triangle soup (3 vertices per triangle) and its one material. */
+struct SecondaryMesh {
+  std::vector<float3> vert;
+  int triangleCount = 0;
+  int materialType = 1; /* 1: reflect, 2: refract, 0: opaque */
+  float reflectivity = 0.95f;
+  float ior = 1.1f;
+  float3 color = {0.95f, 0.95f, 0.95f};
+};
+
+/* SECONDARY_PRIM values (KC/Kd-treeConverter.h:28-30) */
+#define KDGR_SECONDARY_TRI 0
+#define KDGR_SECONDARY_SPHERE 1
+
 /* initCuda (KC/cudaRenderer.cu:2438-2455): device 0. */
 bool initCuda();
 /* renderGaussianWithCudaSetup (KC/cudaRenderer.cu:2557-2703), SECONDARY_RAY 0. */
 void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vector<Gaussian>& gaussians);
+/* The SECONDARY_RAY build's setup (KC/cudaRenderer.h:91-97, cudaRenderer.cu:
+ * 2557-2703 with initSecondaryMesh :2064-2083): the scene plus the secondary
+ * mesh; later frames run the secondary-ray renderer (renderKernelGaussian_
+ * Mesh_Hybrid) against the reference's demo spheres (SECONDARY_PRIM SPHERE,
+ * the committed setting) or the mesh (SECONDARY_PRIM TRI), chosen with
+ * setSecondaryPrimitive.  The mesh vertices are copied. */
+void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vector<Gaussian>& gaussians,
+                                 SecondaryMesh& secondaryMesh);
+/* Run-time stand-in for the reference's compile-time SECONDARY_PRIM
+ * (KDGR_SECONDARY_SPHERE by default); not a reference function. */
+void setSecondaryPrimitive(int prim);
 /* renderGaussianWithCudaFrame (KC/cudaRenderer.cu:3099-3484): plain drop-in
  * (oracle-matching) kernel into d_framebuffer (3*width*height floats, rows
  * flipped); returns 1000 / kernel-ms. */

@@ -49,7 +49,20 @@ int main(int argc, char** argv) {
     g.k_scale = 1 / g.k_scale;
   }
   if (!initCuda()) return 5;
-  renderGaussianWithCudaSetup(obj, gaussians);
+  // KDGR_DEMO_SECONDARY=sphere|tri: the SECONDARY_RAY build's setup with a
+  // mirror square behind the scene (SecondaryMesh defaults), rendering
+  // against the demo spheres or that mesh
+  const char* sec = getenv("KDGR_DEMO_SECONDARY");
+  if (sec && (!strcmp(sec, "sphere") || !strcmp(sec, "tri"))) {
+    SecondaryMesh mesh;
+    const float3 a = {-0.9f, -0.9f, -0.6f}, b = {0.9f, -0.9f, -0.6f}, c = {0.9f, 0.9f, -0.6f}, d = {-0.9f, 0.9f, -0.6f};
+    mesh.vert = {a, b, c, a, c, d};
+    mesh.triangleCount = 2;
+    renderGaussianWithCudaSetup(obj, gaussians, mesh);
+    setSecondaryPrimitive(!strcmp(sec, "tri") ? KDGR_SECONDARY_TRI : KDGR_SECONDARY_SPHERE);
+  } else {
+    renderGaussianWithCudaSetup(obj, gaussians);
+  }
   const int W = atoi(argv[3]), H = atoi(argv[4]);
   Camera cam;
   memset(&cam, 0, sizeof(cam));

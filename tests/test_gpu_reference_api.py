@@ -81,3 +81,35 @@ def test_reference_call_sequence_from_ply(pkg, O, cuda, tmp_path):
     rgb, _, _, _ = O.render(S, cam, w, h)
     np.testing.assert_array_equal(fb, O.to_image(rgb, w, h))
     assert fb.any()
+
+
+@pytest.mark.parametrize("prim", ["sphere", "tri"])
+def test_reference_secondary_ray_build(pkg, O, cuda, fixtures, tmp_path, prim):
+    """The SECONDARY_RAY build's setup (with a SecondaryMesh) and frame: the
+    framebuffer equals the oracle's secondary-ray transcription bit for bit,
+    against the demo spheres or the mesh."""
+    exe = _demo(pkg, tmp_path)
+    fx = fixtures["dense800"]
+    kdgs = tmp_path / "scene.kdgs"
+    pkg.scenes.write_kdgs(str(kdgs), fx.rec)
+    _, cam, w, h, _ = fx.cameras()[0]
+    out = tmp_path / "fb.bin"
+    env = dict(os.environ, KDGR_DEMO_SECONDARY=prim)
+    r = subprocess.run([str(exe), str(kdgs), fx.kdt] + _cam_args(cam, w, h) + [str(out)], capture_output=True,
+                       text=True, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    fb = np.fromfile(out, dtype=np.float32).reshape(h, w, 3)
+    F = pkg.renderer
+    S = O.OracleScene(fx.tree.nodes, fx.tree.offsets, fx.tree.aabb, O.invert_scales(fx.rec))
+    if prim == "sphere":
+        sph = [(tuple(x.center), x.radius, x.material.material, x.material.reflectivity, x.material.ior,
+                tuple(x.material.color)) for x in F.demo_spheres()]
+        want = O.render_hybrid(S, cam, w, h, spheres=sph)
+    else:
+        a, b, c, d = (-0.9, -0.9, -0.6), (0.9, -0.9, -0.6), (0.9, 0.9, -0.6), (-0.9, 0.9, -0.6)
+        tris = np.array([a + b + c, a + c + d], np.float32)
+        m = F.mesh_material_default()
+        want = O.render_hybrid(S, cam, w, h, tris=tris, tri_material=(m.material, m.reflectivity, m.ior,
+                                                                      tuple(m.color)))
+    np.testing.assert_array_equal(fb, O.to_image(want, w, h))
+
