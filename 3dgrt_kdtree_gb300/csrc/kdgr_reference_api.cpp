@@ -6,6 +6,8 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <string>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -33,7 +35,38 @@ void drop_secondary() {
   g_hybrid = false;
 }
 
+std::string g_debug_dir;  // non-empty: per-frame HIT_AND_NODE_COUNT_DEBUG report
+
+// Trace the frame with the oracle-matching kernel and write the report.
+int debug_report_frame(const kdgr_camera& cam, int width, int height, cudaStream_t stream) {
+  const size_t n = (size_t)width * height;
+  kdgr_ray_trace* d_tr = nullptr;
+  float* d_rgb = nullptr;
+  cudaError_t e = cudaMalloc(&d_tr, n * sizeof(kdgr_ray_trace));
+  if (e == cudaSuccess) e = cudaMalloc(&d_rgb, n * 3 * sizeof(float));
+  int rc = e == cudaSuccess ? KDGR_OK : KDGR_ERR_OUT_OF_MEMORY;
+  std::vector<kdgr_ray_trace> h(n);
+  if (rc == KDGR_OK) rc = kdgr_render_trace(g_scene, &cam, width, height, d_rgb, nullptr, nullptr, d_tr, (void*)stream);
+  if (rc == KDGR_OK && cudaStreamSynchronize(stream) != cudaSuccess) rc = KDGR_ERR_CUDA;
+  if (rc == KDGR_OK && cudaMemcpy(h.data(), d_tr, n * sizeof(kdgr_ray_trace), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = KDGR_ERR_CUDA;
+  cudaFree(d_tr);
+  cudaFree(d_rgb);
+  kdgr_debug_stats st;
+  if (rc == KDGR_OK) rc = kdgr_debug_report(h.data(), width, height, g_debug_dir.c_str(), 120.0f, &st);
+  if (rc == KDGR_OK) {
+    printf("\n===========================================\n");
+    printf("avg_node_visits\t\t: %f\n", (double)st.avg[0]);
+    printf("avg_intersection_tests\t: %f\n", (double)st.avg[2]);
+    printf("avg_blend_ops\t\t: %f\n", (double)st.avg[4]);
+    printf("===========================================\n");
+  }
+  return rc;
+}
+
 int render_frame(const kdgr_camera& cam, int width, int height, float* fb, cudaStream_t stream, float* ms) {
+  if (!g_debug_dir.empty() && debug_report_frame(cam, width, height, stream) != KDGR_OK)
+    fprintf(stderr, "[CUDA Error] debug report failed: %s\n", kdgr_last_error());
   if (g_hybrid) {
     kdgr_secondary_t sec = g_secondary_prim == KDGR_SECONDARY_TRI ? g_sec_mesh : g_sec_spheres;
     return kdgr_render_hybrid(g_scene, &cam, width, height, sec, fb, (void*)stream, ms);
@@ -79,6 +112,7 @@ void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vecto
     g_scene = nullptr;
   }
   drop_secondary();
+  if (const char* dd = getenv("KDGR_DEBUG_REPORT_DIR")) g_debug_dir = dd;
   // CompositeObject.AABB is (xmin, xmax, ymin, ymax, zmin, zmax); the scene
   // takes the .kdt order (xmin, ymin, zmin, xmax, ymax, zmax)
   const float aabb[6] = {object.AABB[0], object.AABB[2], object.AABB[4],
@@ -114,6 +148,11 @@ void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vecto
     return;
   }
   g_hybrid = true;
+}
+
+void setDebugReportDir(const char* dir) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_debug_dir = dir ? dir : "";
 }
 
 void setSecondaryPrimitive(int prim) {

@@ -101,6 +101,13 @@ void renderGaussianWithCudaSetup(const CompositeObject& object, const std::vecto
 /* Run-time stand-in for the reference's compile-time SECONDARY_PRIM
  * (KDGR_SECONDARY_SPHERE by default); not a reference function. */
 void setSecondaryPrimitive(int prim);
+/* The HIT_AND_NODE_COUNT_DEBUG build's per-frame report (KC/cudaRenderer.cu:
+ * 3173-3400): with a directory set (here, or through the environment variable
+ * KDGR_DEBUG_REPORT_DIR at setup), every frame also writes renderStats.txt,
+ * render_stats.csv, the heatmaps and the count files there (kdgr_debug_report).
+ * nullptr switches it off.  Not a reference function: the reference selects
+ * this at compile time and writes to "../../output/". */
+void setDebugReportDir(const char* dir);
 /* renderGaussianWithCudaFrame (KC/cudaRenderer.cu:3099-3484): plain drop-in
  * (oracle-matching) kernel into d_framebuffer (3*width*height floats, rows
  * flipped); returns 1000 / kernel-ms. */

@@ -113,3 +113,29 @@ def test_reference_secondary_ray_build(pkg, O, cuda, fixtures, tmp_path, prim):
                                                                       tuple(m.color)))
     np.testing.assert_array_equal(fb, O.to_image(want, w, h))
 
+
+
+def test_reference_frame_writes_debug_report(pkg, O, cuda, fixtures, tmp_path):
+    """With KDGR_DEBUG_REPORT_DIR set (the HIT_AND_NODE_COUNT_DEBUG build),
+    a frame writes the reference's report files; they equal the report of
+    the oracle's traces, file for file."""
+    exe = _demo(pkg, tmp_path)
+    fx = fixtures["cluster2k"]
+    kdgs = tmp_path / "scene.kdgs"
+    pkg.scenes.write_kdgs(str(kdgs), fx.rec)
+    _, cam, w, h, _ = fx.cameras()[1]
+    out_dir = tmp_path / "report"
+    out_dir.mkdir()
+    env = dict(os.environ, KDGR_DEBUG_REPORT_DIR=str(out_dir))
+    r = subprocess.run([str(exe), str(kdgs), fx.kdt] + _cam_args(cam, w, h) + [str(tmp_path / "fb.bin")],
+                       capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    S = O.OracleScene(fx.tree.nodes, fx.tree.offsets, fx.tree.aabb, O.invert_scales(fx.rec))
+    _, _, _, tr = O.render(S, cam, w, h, trace=True)
+    want_dir = tmp_path / "want"
+    want_dir.mkdir()
+    pkg.renderer.debug_report(tr, w, h, out_dir=str(want_dir))
+    names = sorted(os.listdir(want_dir))
+    assert len(names) == 16 and sorted(os.listdir(out_dir)) == names
+    for n in names:
+        assert (out_dir / n).read_bytes() == (want_dir / n).read_bytes(), n
