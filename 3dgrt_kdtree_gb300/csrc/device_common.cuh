@@ -36,26 +36,25 @@ struct ExactView {
 };
 
 // Device arrays of the fast forms.
-//   nodes:   re-laid-out tree: the top `top_nodes` nodes in breadth-first
-//            order (staged in shared memory), the rest depth-first by subtree;
-//            children stay pairwise adjacent.  Leaf words are unchanged.
-//   test:    3 x float4 per Gaussian: rows of M = diag(1/s) R^T with
-//            b = M mu folded in: (M0, b0) (M1, b1) (M2, b2);
-//   opacity: 1 float per Gaussian;
-//   sh:      FP32 coefficient-major (shared with ExactView);
-//   packed:  2 x uint4 per Gaussian: (mu.xyz f32, opacity f32 with the sign
-//            bit set when the Gaussian is anisotropic) and (half2 1/s.xy,
-//            half2 1/s.z|0, half2 q.wx, half2 q.yz);
-//   sh_bf16: 6 x uint4 per Gaussian, BF16 coefficient-major;
-//   aniso_idx / aniso: for Gaussians with scale ratio > 1e3, the index into
-//            3 x float4 (M0,b0)(M1,b1)(M2,b2) from the FP64 upload precompute.
+//   nodes:      re-laid-out tree: the top levels breadth-first, the rest
+//               depth-first by subtree; children stay pairwise adjacent.
+//               Leaf words are unchanged.
+//   offsets:    leaf Gaussian-ID lists (read for accepted hits only);
+//   opacity:    1 float per Gaussian;
+//   sh:         FP32 coefficient-major (shared with ExactView);
+//   sh_bf16:    6 x uint4 per Gaussian, BF16 coefficient-major;
+//   aniso_idx / aniso: for flagged Gaussians (scale ratio > 1e3, or factors
+//               beyond FP16), the index into 3 x float4 (M0,b0)(M1,b1)(M2,b2)
+//               from the FP64 upload precompute;
+//   leaf_pairs: FP32 form, per pair of leaf entries (2p, 2p+1) the rows of
+//               M = diag(1/s) R^T and b = M mu interleaved lo/hi, 6 x float4;
+//   leaf_packed: packed form, per leaf entry 2 x uint4: (mu.xyz f32, half2
+//               (M22, flag)) and the other eight entries of M as four half2.
 struct FastView {
   const uint2* nodes;
   const uint32_t* offsets;
-  const float4* test;
   const float* opacity;
   const float4* sh;
-  const uint4* packed;
   const uint4* sh_bf16;
   const uint32_t* aniso_idx;
   const float4* aniso;

@@ -133,10 +133,8 @@ kdgr::FastView kdgr_scene_s::fast_view() const {
   FastView v;
   v.nodes = d_nodes_fast;
   v.offsets = d_offsets;
-  v.test = d_test_fast;
   v.opacity = d_opacity;
   v.sh = d_sh;
-  v.packed = d_packed;
   v.sh_bf16 = d_sh_bf16;
   v.aniso_idx = d_aniso_idx;
   v.aniso = d_aniso;
@@ -309,16 +307,17 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
       }
       op[i] = r[3];
     }
-    s->d_test_fast = A.alloc<float4>(3 * (size_t)n);
     s->d_opacity = A.alloc<float>(n);
-    if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (fast)");
-    if (cudaMemcpy(s->d_test_fast, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(s->d_opacity, op.data(), op.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
-      return fail("kdgr_scene_create: upload (fast)");
     s->d_leaf_pairs = A.alloc<float4>(6 * (((size_t)n_offsets + 1) / 2 + 1));
-    if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (leaf records)");
-    if (build_leaf_pairs(s->d_offsets, n_offsets, s->d_test_fast, s->d_leaf_pairs) != cudaSuccess)
-      return fail("kdgr_scene_create: leaf records (fast)");
+    if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (fast)");
+    // the per-Gaussian records are staging only: the kernels read the leaf-order pairs
+    float4* d_stage = nullptr;
+    cudaError_t e = cudaMalloc(&d_stage, tf.size() * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(d_stage, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_opacity, op.data(), op.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = build_leaf_pairs(s->d_offsets, n_offsets, d_stage, s->d_leaf_pairs);
+    if (d_stage) cudaFree(d_stage);
+    if (e != cudaSuccess) return fail("kdgr_scene_create: upload (fast)");
   }
   if (forms & KDGR_FORM_PACKED) {
     rc = pack_precision(s.get(), g, giscl.data(), sh.data(), A);
@@ -336,7 +335,7 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
 int kdgr_scene_destroy(kdgr_scene_t s) {
   if (!s) return KDGR_ERR_INVALID_ARG;
   void* ps[] = {s->d_nodes,     s->d_offsets, s->d_test,      s->d_sh,          s->d_nodes_fast,
-                s->d_test_fast, s->d_opacity, s->d_packed,    s->d_sh_bf16,     s->d_aniso_idx,
+                s->d_opacity,   s->d_sh_bf16,     s->d_aniso_idx,
                 s->d_aniso,     s->d_leaf_pairs, s->d_leaf_packed, s->d_status};
   cudaError_t first = cudaSuccess;
   for (void* p : ps)

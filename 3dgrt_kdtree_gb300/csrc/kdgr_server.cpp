@@ -282,7 +282,7 @@ void kdgr_server_s::completer() {
 }
 
 static uint64_t estimate_scene_bytes(uint32_t n_nodes, uint32_t n_offsets, uint32_t n, bool packed) {
-  const uint64_t per = packed ? (32 + 96 + 4) : (48 + 4 + 192);
+  const uint64_t per = packed ? (96 + 4 + 4) : (4 + 192);  // SH, opacity (+ aniso index)
   const uint64_t per_entry = 4 + (packed ? 32 : 48);  // ID + leaf-order record
   return 8ull * n_nodes + per_entry * n_offsets + per * n;
 }

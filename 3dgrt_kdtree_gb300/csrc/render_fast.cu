@@ -889,13 +889,14 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
         cudaMemcpy(s->d_opacity, opac.data(), n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
       return cuda_fail(cudaErrorUnknown, "kdgr_scene_create: opacity upload (packed)");
   }
-  s->d_packed = A.alloc<uint4>(2 * n);
+  uint4* d_stage = nullptr;  // per-Gaussian packed records: staging for the leaf-order copy
   s->d_sh_bf16 = A.alloc<uint4>(6 * n);
   s->d_aniso_idx = A.alloc<uint32_t>(n);
   s->d_aniso = A.alloc<float4>(3 * (size_t)(n_aniso ? n_aniso : 1));
   float* d_src = nullptr;
   if (A.err != cudaSuccess) return cuda_fail(A.err, "kdgr_scene_create: cudaMalloc (packed)");
-  cudaError_t e = cudaMemcpy(s->d_packed, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMalloc(&d_stage, packed.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(d_stage, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->d_sh_bf16, shb.data(), shb.size() * 2, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->d_aniso_idx, aidx.data(), aidx.size() * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && n_aniso) {
@@ -908,12 +909,14 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (d_src) cudaFree(d_src);
   }
+  if (e == cudaSuccess) {
+    s->n_aniso = n_aniso;
+    s->d_leaf_packed = A.alloc<uint4>(2 * (size_t)(s->n_offsets ? s->n_offsets : 1));
+    e = A.err;
+  }
+  if (e == cudaSuccess) e = gather_leaf_records(s->d_offsets, s->n_offsets, d_stage, 2, s->d_leaf_packed);
+  if (d_stage) cudaFree(d_stage);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed upload");
-  s->n_aniso = n_aniso;
-  s->d_leaf_packed = A.alloc<uint4>(2 * (size_t)(s->n_offsets ? s->n_offsets : 1));
-  if (A.err != cudaSuccess) return cuda_fail(A.err, "kdgr_scene_create: cudaMalloc (packed leaf records)");
-  e = gather_leaf_records(s->d_offsets, s->n_offsets, s->d_packed, 2, s->d_leaf_packed);
-  if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed leaf records");
   return KDGR_OK;
 }
 

@@ -24,9 +24,7 @@ struct kdgr_scene_s {
   // fast forms
   uint2* d_nodes_fast = nullptr;
   uint32_t top_nodes = 0;
-  float4* d_test_fast = nullptr;
   float* d_opacity = nullptr;
-  uint4* d_packed = nullptr;
   uint4* d_sh_bf16 = nullptr;
   uint32_t* d_aniso_idx = nullptr;
   float4* d_aniso = nullptr;
