@@ -134,3 +134,42 @@ def test_batch_config_errors(pkg, cuda, fixtures):
     with pytest.raises(pkg.capi.KdgrError):
         scene.render_batch(views, 1, rgb)  # no fast arrays materialised
     scene.close()
+
+
+KAT_CASES = {
+    "analytic": lambda kat: (kat.analytic_single(), 32, 24),
+    "straddle": lambda kat: ((lambda t: (t[0], t[2], t[3]))(kat.straddle()), 16, 16),
+    "comb": lambda kat: ((lambda t: (t[0], t[2], t[3]))(kat.comb(20)), 8, 8),
+    "ties": lambda kat: (kat.ties(20), 8, 8),
+    "big_leaf": lambda kat: (kat.big_leaf(100), 16, 16),
+    "empty": lambda kat: (kat.empty(), 8, 8),
+    "miss": lambda kat: (kat.miss(), 8, 8),
+}
+
+
+@pytest.mark.parametrize("case", sorted(KAT_CASES))
+def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
+    """The batching and precision forms on the hand-built scenes: a stack
+    deeper than the ring (restarts), 20 equal-t hits in one leaf (more than
+    the hit buffer: re-scan passes), a 100-candidate leaf, a Gaussian across
+    a split, an empty scene and a missed box; both within the accuracy bar
+    of the FP64 oracle, and the FP32 form equal across every schedule."""
+    import kat
+    (tree, rec, cam), W, H = KAT_CASES[case](kat)
+    F = pkg.renderer
+    scene = F.Scene(tree, rec, forms=F.FORM_FAST | F.FORM_PACKED)
+    r64, a64, _, _ = oracle_image(O, tree, rec, cam, W, H, precision="f64")
+    for prec in (0, 1):
+        rgb, a = fast_image(pkg, cuda, scene, cam, W, H, prec)
+        assert rmse(rgb, r64) <= RMSE_TOL, (prec, rmse(rgb, r64))
+        assert rmse(a, a64) <= RMSE_TOL
+    views, total, _ = F.make_views([(cam, W, H)])
+    ref = torch.zeros(total * 3, device=cuda)
+    scene.render_batch(views, 1, ref)
+    for sched, kb in [(0, 4), (1, 8), (2, 4)]:
+        out = torch.full_like(ref, -1.0)
+        scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, 0, kb))
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), ref.cpu().numpy())
+    assert scene.status() == 0
+    scene.close()
