@@ -62,9 +62,6 @@ constexpr int kBlockW = 16, kBlockH = 8;  // pixels per CTA block (4 warps of 8x
 #ifndef KDGR_FAST_PIPE
 #define KDGR_FAST_PIPE 2
 #endif
-#ifndef KDGR_FAST_PREFETCH
-#define KDGR_FAST_PREFETCH 0
-#endif
 #ifndef KDGR_FAST_STACK
 #define KDGR_FAST_STACK 12
 #endif
@@ -195,10 +192,17 @@ __device__ __forceinline__ PairRec load_pair(const FastView& S, uint32_t p) {
 // gray = |grdu x gro|^2 / |grdu|^2) for both entries of a pair.  Works with
 // ng = b - M o = -gro, so t* = (grdu . ng) / |grdu|^2 and the cross product
 // keeps its length.  Returns the pass mask (bit 0: entry 2p, bit 1: 2p+1).
-__device__ __forceinline__ unsigned test_pair(const PairRec& r, F3 o, F3 d, float t_near, float t_far, float t[2],
+// Ray constants of the pair test, broadcast to both halves once per leaf.
+struct Ray2 {
+  f2 nox, noy, noz, dx, dy, dz;
+};
+__device__ __forceinline__ Ray2 ray2(F3 o, F3 d) {
+  return Ray2{bcast2(-o.x), bcast2(-o.y), bcast2(-o.z), bcast2(d.x), bcast2(d.y), bcast2(d.z)};
+}
+
+__device__ __forceinline__ unsigned test_pair(const PairRec& r, const Ray2& w, float t_near, float t_far, float t[2],
                                               float g[2]) {
-  const f2 nox = bcast2(-o.x), noy = bcast2(-o.y), noz = bcast2(-o.z);
-  const f2 dx = bcast2(d.x), dy = bcast2(d.y), dz = bcast2(d.z);
+  const f2 nox = w.nox, noy = w.noy, noz = w.noz, dx = w.dx, dy = w.dy, dz = w.dz;
   f2 ng[3], gd[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -419,18 +423,11 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     bool overflow = false;
     if constexpr (!PACKED) {
       const uint32_t end = base + cnt;
-#if KDGR_FAST_PREFETCH
-      PairRec nxt = load_pair(S, (base & ~1u) >> 1);
-#endif
+      const Ray2 w = ray2(R.o, R.d);
       for (uint32_t e = base & ~1u; e < end; e += 2) {
-#if KDGR_FAST_PREFETCH
-        const PairRec pr = nxt;
-        if (e + 2 < end) nxt = load_pair(S, (e + 2) >> 1);  // next pair in flight during this test
-#else
         const PairRec pr = load_pair(S, e >> 1);
-#endif
         float t2[2], g2[2];
-        unsigned m = test_pair(pr, R.o, R.d, R.t_near, R.t_far, t2, g2);
+        unsigned m = test_pair(pr, w, R.t_near, R.t_far, t2, g2);
         if (e < base) m &= 2u;     // low half belongs to the previous leaf
         if (e + 1 >= end) m &= 1u;  // high half belongs to the next leaf
 #pragma unroll
