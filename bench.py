@@ -420,7 +420,7 @@ def run_serving(args):
 
 
 # ------------------------------------------------------------------ CPU arm
-def cpu_sample(tree, rec, cams, seconds: float, threads: int = 0):
+def cpu_sample(tree, rec, cams, seconds: float, threads: int = 0, precision: str = "f32"):
     """Render a strided ray sample of every view with the oracle (CPU), sized
     to about `seconds` of work.  Returns (Mrays/s, rays, stride, threads)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -433,7 +433,7 @@ def cpu_sample(tree, rec, cams, seconds: float, threads: int = 0):
         t = time.time()
         for cam, w, h in cams:
             pix = np.arange(0, w * h, stride, dtype=np.uint32)
-            O.render(S, cam, w, h, pixels=pix, threads=nthr)
+            O.render(S, cam, w, h, pixels=pix, threads=nthr, precision=precision)
             n += pix.size
         return n, time.time() - t
 
@@ -570,9 +570,32 @@ def run_hybrid(args):
 
 def cpu_baseline(tree, rec, cams, seconds):
     mr, n, stride, nthr, dt = cpu_sample(tree, rec, cams, seconds)
+    mr1, n1, _, _, dt1 = cpu_sample(tree, rec, cams, max(1.0, seconds / 4), threads=1)
+    mr64, n64, _, _, dt64 = cpu_sample(tree, rec, cams, max(1.0, seconds / 4), precision="f64")
     return {"value": round(mr, 4), "unit": UNIT, "cores": nthr, "kind": "port",
             "sample": f"every {stride}th ray of each view ({n} rays, {dt:.1f}s), oracle FP32 transcription "
-                      f"of cudaRenderer.cu with OpenMP over rays"}
+                      f"of cudaRenderer.cu with OpenMP over rays",
+            "single_thread_value": round(mr1, 4), "single_thread_sample": f"{n1} rays, {dt1:.1f}s",
+            "fp64_value": round(mr64, 4), "fp64_sample": f"{n64} rays, {dt64:.1f}s, {nthr} threads",
+            "cpu_model": cpu_model()}
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def run_reference(args):
