@@ -140,11 +140,16 @@ def algorithmic_bytes(tr, b_test: int, b_blend: int, b_out: int) -> float:
 
 
 def load_traffic():
-    p = os.path.join(REPO, "profiles", "traffic.json")
+    """profiles/traffic.txt: `config:form bytes` lines (# comments)."""
+    out = {}
     try:
-        return json.load(open(p))
-    except Exception:
+        for line in open(os.path.join(REPO, "profiles", "traffic.txt")):
+            f = line.split("#", 1)[0].split()
+            if len(f) == 2:
+                out[f[0]] = int(f[1])
+    except (OSError, ValueError):
         return {}
+    return out
 
 
 # ------------------------------------------------------------------ our arm
