@@ -21,12 +21,12 @@
 //   * FP32 form: leaf entries are stored in interleaved pairs and tested two
 //     at a time with Blackwell's packed FP32x2 instructions
 //     (fma/mul/sub.rn.f32x2), half the arithmetic instructions per test;
-//   * a leaf's candidates are fetched kPipe at a time (all record loads in
-//     flight before the first test), multiplying the memory-level
-//     parallelism of the latency-bound candidate loop;
-//   * pixels are handed out in spatially coherent units (8x4 warp tiles or
-//     16x8 CTA blocks) so the rays sharing an SM's L1 are neighbours; the
-//     autotuner picks the schedule and the register cap (occupancy).
+//   * the precision form reads a leaf's candidates kPipe at a time (all
+//     record loads in flight before the first test);
+//   * pixels are handed out in spatially coherent units (8x4 warp tiles,
+//     16x8 CTA blocks, or CTA blocks from per-SM contiguous strips) so the
+//     rays sharing an SM's L1 are neighbours; the autotuner picks the
+//     schedule, the register cap (occupancy) and the hit-buffer size.
 //   * precision form: FP16 rows of M with an FP32 mean and BF16 SH (32 + 96
 //     bytes per Gaussian instead of 48 + 192); Gaussians whose scale ratio
 //     exceeds 1e3 (or whose factors leave the FP16 range) read FP32 factors
