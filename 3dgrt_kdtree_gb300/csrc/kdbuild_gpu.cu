@@ -199,6 +199,37 @@ __device__ __forceinline__ uint32_t count_le(const uint64_t* k, size_t b, uint32
   return lo;
 }
 
+// The same counts with the answer known to lie in [lo, hi].
+__device__ __forceinline__ uint32_t count_less_in(const uint64_t* k, size_t b, uint32_t lo, uint32_t hi, float p) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (key_pos(k[b + mid]) < p) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ uint32_t count_le_in(const uint64_t* k, size_t b, uint32_t lo, uint32_t hi, float p) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (key_pos(k[b + mid]) <= p) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Bounds for the counts of a warp whose 32 lanes hold consecutive sorted
+// candidates of one segment: every lane's count lies between lane 0's
+// count_less and lane 31's count_le, found once by those two lanes.
+struct Bracket {
+  uint32_t lo, hi;
+};
+__device__ __forceinline__ Bracket warp_bracket(const uint64_t* k, size_t b, uint32_t n, float p, int lane) {
+  uint32_t v = 0;
+  if (lane == 0) v = count_less(k, b, n, p);
+  if (lane == 31) v = count_le(k, b, n, p);
+  return Bracket{__shfl_sync(0xFFFFFFFFu, v, 0), __shfl_sync(0xFFFFFFFFu, v, 31)};
+}
+
 __device__ __forceinline__ float ref_min(float a, float b) { return a < b ? a : b; }
 __device__ __forceinline__ float ref_max(float a, float b) { return a > b ? a : b; }
 
@@ -402,9 +433,30 @@ __global__ void k_eval(const uint64_t* __restrict__ kc, size_t n_cand, size_t eT
                        const uint32_t* __restrict__ pl_cnt, const NodeConst* __restrict__ nc, uint32_t N, Params P,
                        double* cost_out, uint8_t* side_out, unsigned long long* best_bits) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
   double cost = __longlong_as_double(0x7FF0000000000000ll);  // +inf: not a candidate
   uint8_t side = 0;
   uint32_t seg = kNone;
+  // warp-wide brackets when all 32 lanes sit in one (axis, node) segment
+  uint32_t my_seg = kNone;
+  float my_p = 0.f;
+  if (i < n_cand) {
+    int a0;
+    uint32_t n0;
+    decode(kc[i], nb, &a0, &n0);
+    my_seg = (uint32_t)a0 * N + n0;
+    my_p = key_pos(kc[i]);
+  }
+  const bool uniform = __all_sync(0xFFFFFFFFu, my_seg == __shfl_sync(0xFFFFFFFFu, my_seg, 0) && my_seg != kNone);
+  Bracket bmin{0, 0}, bmax{0, 0}, bpl{0, 0};
+  if (uniform) {
+    const uint32_t a0 = my_seg / N, n0 = my_seg % N;
+    const uint32_t G0 = nc[n0].G;
+    const size_t gb0 = (size_t)a0 * eGT + grb[n0];
+    bmin = warp_bracket(kmin, gb0, G0, my_p, lane);
+    bmax = warp_bracket(kmax, gb0, G0, my_p, lane);
+    bpl = warp_bracket(kpl, plb[my_seg], pl_cnt[my_seg], my_p, lane);
+  }
   if (i < n_cand) {
     const uint64_t k = kc[i];
     int a;
@@ -417,13 +469,23 @@ __global__ void k_eval(const uint64_t* __restrict__ kc, size_t n_cand, size_t eT
     if (head && p > c.lim_lo[a] && p < c.lim_hi[a]) {
       const uint32_t G = c.G;
       const size_t gb = (size_t)a * eGT + grb[n];
-      const uint32_t open = count_less(kmin, gb, G, p);
-      const uint32_t close = count_less(kmax, gb, G, p);
-      const uint32_t eq_max = count_le(kmax, gb, G, p) - close;
       const size_t pb = plb[(size_t)a * N + n];
       const uint32_t pn = pl_cnt[(size_t)a * N + n];
-      const uint32_t pl_lt = count_less(kpl, pb, pn, p);
-      const int num_planars = (int)(count_le(kpl, pb, pn, p) - pl_lt);
+      uint32_t open, close, eq_max, pl_lt, pl_le;
+      if (uniform) {
+        open = count_less_in(kmin, gb, bmin.lo, bmin.hi, p);
+        close = count_less_in(kmax, gb, bmax.lo, bmax.hi, p);
+        eq_max = count_le_in(kmax, gb, close, bmax.hi, p) - close;
+        pl_lt = count_less_in(kpl, pb, bpl.lo, bpl.hi, p);
+        pl_le = count_le_in(kpl, pb, pl_lt, bpl.hi, p);
+      } else {
+        open = count_less(kmin, gb, G, p);
+        close = count_less(kmax, gb, G, p);
+        eq_max = count_le(kmax, gb, G, p) - close;
+        pl_lt = count_less(kpl, pb, pn, p);
+        pl_le = count_le(kpl, pb, pn, p);
+      }
+      const int num_planars = (int)(pl_le - pl_lt);
       const int local_close = (int)eq_max - num_planars;
 
       const double extent_l = double(p) - c.cell_min[a];
