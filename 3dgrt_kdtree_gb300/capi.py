@@ -48,7 +48,7 @@ class Gaussians(ctypes.Structure):
 
 class BuildStats(ctypes.Structure):
     _fields_ = [("proxy_s", ctypes.c_double), ("build_s", ctypes.c_double), ("n_triangles", ctypes.c_uint64),
-                ("n_valid", ctypes.c_uint32)]
+                ("n_valid", ctypes.c_uint32), ("serialize_s", ctypes.c_double)]
 
 
 class RayTrace(ctypes.Structure):

@@ -40,6 +40,7 @@
 #include <cub/cub.cuh>
 
 #include <cfloat>
+#include <cstdio>
 #include <chrono>
 #include <cstdint>
 #include <cstring>
@@ -67,8 +68,12 @@ struct Params {
 };
 
 // ------------------------------------------------------------ device buffers
+// The build's stream and its own memory pool: the pool keeps what it has
+// mapped until the build ends (the device's default pool would hand it back
+// at every stream synchronisation, and the level loop synchronises often).
 struct Stream {
   cudaStream_t s = nullptr;
+  cudaMemPool_t pool = nullptr;
   cudaError_t err = cudaSuccess;
   void check(cudaError_t e) {
     if (err == cudaSuccess && e != cudaSuccess) err = e;
@@ -86,7 +91,7 @@ struct DBuf {
     release();
     st = &s;
     n = count;
-    if (count) st->check(cudaMallocAsync(&p, count * sizeof(T), st->s));
+    if (count) st->check(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&p), count * sizeof(T), st->pool, st->s));
   }
   void release() {
     if (p && st) cudaFreeAsync(p, st->s);
@@ -802,8 +807,20 @@ int build_tree_gpu(const float* gauss, uint32_t n, const BuildParams& bp, HostTr
     err = "every Gaussian is below the opacity cut; nothing to build";
     return KDGR_ERR_INVALID_ARG;
   }
+  bool limit_hit = false;
   Stream S;
   S.check(cudaStreamCreateWithFlags(&S.s, cudaStreamNonBlocking));
+  {
+    int dev = 0;
+    S.check(cudaGetDevice(&dev));
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    S.check(cudaMemPoolCreate(&S.pool, &props));
+    uint64_t keep = UINT64_MAX;
+    if (S.pool) S.check(cudaMemPoolSetAttribute(S.pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  }
   S.check(cudaMemcpyToSymbolAsync(c_ico_v, kIcosaVerts, sizeof kIcosaVerts, 0, cudaMemcpyHostToDevice, S.s));
   S.check(cudaMemcpyToSymbolAsync(c_ico_f, kIcosaFaces, sizeof kIcosaFaces, 0, cudaMemcpyHostToDevice, S.s));
   const Params P{bp.max_level, bp.force_split, bp.isect_cost, bp.sah_mode, bp.sort_cost};
@@ -836,19 +853,35 @@ int build_tree_gpu(const float* gauss, uint32_t n, const BuildParams& bp, HostTr
     const uint32_t tb0[2] = {0, (uint32_t)T};
     S.check(cudaMemcpyAsync(tb.p, tb0, 8, cudaMemcpyHostToDevice, S.s));
     S.check(cudaStreamSynchronize(S.s));
-    if (T > 0xFFFFFFF0ull) {
+    uint32_t N = 1;
+    if (T > 0xFFFFFFF0ull) {  // leave through the normal exit so every buffer is freed first
       err = "more than 2^32 proxy triangles";
-      cudaStreamDestroy(S.s);
-      return KDGR_ERR_LIMIT;
+      limit_hit = true;
+      N = 0;
     }
     auto t1 = clk::now();
     if (stats) stats->proxy_s = std::chrono::duration<double>(t1 - t0).count();
     if (stats) stats->n_triangles = T;
     if (stats) stats->n_valid = n_valid;
 
-    uint32_t N = 1;
     uint32_t base = 0;  // global BFS index of the level's first node
     for (int level = 0; N > 0 && S.err == cudaSuccess; ++level) {
+#ifdef KDGR_BUILD_TRACE  // compile-time diagnostic: per-level wall time and sizes on stderr
+      const auto lt0 = clk::now();
+      struct LevelTrace {
+        std::chrono::steady_clock::time_point t0;
+        int level;
+        const uint32_t* n;
+        const size_t* t;
+        ~LevelTrace() {
+          fprintf(stderr, "[kdbuild_gpu] level %d: %u nodes, %zu triangles, %.2f ms\n", level, *n, *t,
+                  std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+        }
+      };
+      const uint32_t n_in = N;
+      const size_t t_in = T;
+      LevelTrace trace_guard{lt0, level, &n_in, &t_in};
+#endif
       depth = (uint32_t)level;
       int nb = 1;
       while ((1u << nb) < N) ++nb;
@@ -969,7 +1002,7 @@ int build_tree_gpu(const float* gauss, uint32_t n, const BuildParams& bp, HostTr
       const size_t T2 = read_one(S, ntb.p + N2);
       if (T2 > 0xFFFFFFF0ull) {
         err = "more than 2^32 triangle references in one level";
-        S.err = cudaErrorMemoryAllocation;
+        limit_hit = true;
         break;
       }
       TriSet nxt;
@@ -997,6 +1030,8 @@ int build_tree_gpu(const float* gauss, uint32_t n, const BuildParams& bp, HostTr
   S.check(cudaStreamSynchronize(S.s));
   const cudaError_t e = S.err;
   cudaStreamDestroy(S.s);
+  if (S.pool) cudaMemPoolDestroy(S.pool);
+  if (limit_hit && e == cudaSuccess) return KDGR_ERR_LIMIT;
   if (e != cudaSuccess) {
     if (err.empty()) err = std::string("CUDA error in the device build: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? KDGR_ERR_OUT_OF_MEMORY : KDGR_ERR_CUDA;

@@ -299,6 +299,7 @@ int kdgr_build_tree(const float* gaussians, uint32_t n_gaussians, const kdgr_bui
     stats->build_s = bs.build_s + bs.serialize_s;
     stats->n_triangles = bs.n_triangles;
     stats->n_valid = bs.n_valid;
+    stats->serialize_s = bs.serialize_s;
   }
   return fill_out(t, n_gaussians, out);
 }
@@ -362,6 +363,7 @@ int kdgr_build_tree_gpu(const float* gaussians, uint32_t n_gaussians, const kdgr
     stats->build_s = bs.build_s + bs.serialize_s;
     stats->n_triangles = bs.n_triangles;
     stats->n_valid = bs.n_valid;
+    stats->serialize_s = bs.serialize_s;
   }
   return fill_out(t, n_gaussians, out);
 }

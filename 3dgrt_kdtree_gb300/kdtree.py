@@ -59,7 +59,8 @@ def build(gaussians: np.ndarray, max_level: int = 24, force_split: int = 16, ise
     capi.check(getattr(L, fn)(rec.ctypes.data, rec.shape[0], ctypes.byref(p), ctypes.byref(t), ctypes.byref(s)),
                fn)
     tree = _take(t)
-    tree.stats = {"proxy_s": s.proxy_s, "build_s": s.build_s, "n_triangles": int(s.n_triangles),
+    tree.stats = {"proxy_s": s.proxy_s, "build_s": s.build_s, "serialize_s": s.serialize_s,
+                  "n_triangles": int(s.n_triangles),
                   "n_valid": int(s.n_valid)}
     return tree
 

@@ -86,9 +86,10 @@ typedef struct {
 
 typedef struct {
   double proxy_s;
-  double build_s;
+  double build_s;      /* split search and partition, including serialize_s */
   uint64_t n_triangles;
   uint32_t n_valid;
+  double serialize_s;  /* numbering the nodes in the reference's order and copying the leaf lists out */
 } kdgr_build_stats;
 
 void kdgr_build_params_default(kdgr_build_params* params);
