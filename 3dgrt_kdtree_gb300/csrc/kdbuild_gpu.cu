@@ -322,13 +322,22 @@ __global__ void k_run_heads(const uint32_t* __restrict__ gid, const uint32_t* __
 }
 
 __global__ void k_run_scatter(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ ridx,
-                              const uint32_t* __restrict__ node, size_t T, uint32_t* run_start, uint32_t* run_node,
-                              uint32_t* G) {
+                              const uint32_t* __restrict__ node, size_t T, uint32_t* run_start, uint32_t* run_node) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T || !flag[t]) return;
   run_start[ridx[t]] = (uint32_t)t;
   run_node[ridx[t]] = node[t];
-  atomicAdd(&G[node[t]], 1u);
+}
+
+// First run of every node: runs are ordered by node, so node n's runs start
+// at the run index of its first triangle (an empty node gets the next node's
+// first run), and G[n] = rb[n+1] - rb[n].  rb[N] = R.
+__global__ void k_node_runs(const uint32_t* __restrict__ tb, const uint32_t* __restrict__ ridx, uint32_t N,
+                            uint32_t* rb, uint32_t* G) {
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n > N) return;
+  rb[n] = ridx[tb[n]];
+  if (n < N) G[n] = ridx[tb[n + 1]] - ridx[tb[n]];
 }
 
 struct NodeConst {
@@ -409,19 +418,68 @@ __global__ void k_run_bounds(const uint32_t* __restrict__ run_start, const uint3
   }
 }
 
-__global__ void k_cand_keys(const float* __restrict__ lo, const float* __restrict__ hi, size_t cap, size_t T,
-                            const uint32_t* __restrict__ node, const uint32_t* __restrict__ tb,
-                            const NodeConst* __restrict__ nc, const uint32_t* __restrict__ ctb, size_t eTT, int nb,
-                            uint64_t* kc) {
-  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= T) return;
-  const uint32_t n = node[t];
-  if (!nc[n].elig) return;
-  const size_t slot = 2 * ((size_t)ctb[n] + (t - tb[n]));
-  for (int a = 0; a < 3; ++a) {
-    kc[a * 2 * eTT + slot] = make_key(a, n, lo[a * cap + t], nb);
-    kc[a * 2 * eTT + slot + 1] = make_key(a, n, hi[a * cap + t], nb);
+// Candidate positions of a run (one Gaussian's triangles in one node): the
+// lo and hi edges of its triangles on axis a, bitwise duplicates removed
+// (-0 and +0 stay distinct, as in the full sorted list; the sweep groups
+// equal positions anyway, so the scored candidates are the same).  A run
+// holds at most 20 triangles; longer runs (not produced by the proxy mesh)
+// keep every edge.
+constexpr int kRunEdges = 64;
+
+template <bool WRITE>
+__device__ __forceinline__ uint32_t run_edges(const float* __restrict__ lo, const float* __restrict__ hi, size_t cap,
+                                              uint32_t t0, uint32_t t1, int a, uint32_t n, int nb, uint64_t* out) {
+  const uint32_t m = 2 * (t1 - t0);
+  uint32_t count = 0;
+  if (m > (uint32_t)kRunEdges) {
+    for (uint32_t t = t0; t < t1; ++t) {
+      if (WRITE) {
+        out[count] = make_key(a, n, lo[a * cap + t], nb);
+        out[count + 1] = make_key(a, n, hi[a * cap + t], nb);
+      }
+      count += 2;
+    }
+    return count;
   }
+  uint32_t v[kRunEdges];
+  for (uint32_t t = t0; t < t1; ++t) {
+    v[2 * (t - t0)] = __float_as_uint(lo[a * cap + t]);
+    v[2 * (t - t0) + 1] = __float_as_uint(hi[a * cap + t]);
+  }
+  for (uint32_t j = 0; j < m; ++j) {
+    bool seen = false;
+    for (uint32_t k = 0; k < j && !seen; ++k) seen = v[k] == v[j];
+    if (seen) continue;
+    if (WRITE) out[count] = make_key(a, n, __uint_as_float(v[j]), nb);
+    ++count;
+  }
+  return count;
+}
+
+// Pass 1: distinct candidate count per (axis, run); 0 for runs of nodes that
+// are not split candidates.
+__global__ void k_run_cand_count(const uint32_t* __restrict__ run_start, const uint32_t* __restrict__ run_node,
+                                 uint32_t R, size_t T, const float* __restrict__ lo, const float* __restrict__ hi,
+                                 size_t cap, const NodeConst* __restrict__ nc, unsigned long long* cnt) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const uint32_t n = run_node[r];
+  const uint32_t t0 = run_start[r], t1 = r + 1 < R ? run_start[r + 1] : (uint32_t)T;
+  for (int a = 0; a < 3; ++a)
+    cnt[(size_t)a * R + r] = nc[n].elig ? run_edges<false>(lo, hi, cap, t0, t1, a, n, 0, nullptr) : 0u;
+}
+
+// Pass 2: the keys, at the scanned offsets.
+__global__ void k_run_cand_write(const uint32_t* __restrict__ run_start, const uint32_t* __restrict__ run_node,
+                                 uint32_t R, size_t T, const float* __restrict__ lo, const float* __restrict__ hi,
+                                 size_t cap, const NodeConst* __restrict__ nc, const unsigned long long* __restrict__ off,
+                                 int nb, uint64_t* kc) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const uint32_t n = run_node[r];
+  if (!nc[n].elig) return;
+  const uint32_t t0 = run_start[r], t1 = r + 1 < R ? run_start[r + 1] : (uint32_t)T;
+  for (int a = 0; a < 3; ++a) run_edges<true>(lo, hi, cap, t0, t1, a, n, nb, kc + off[(size_t)a * R + r]);
 }
 
 __device__ __forceinline__ void decode(uint64_t k, int nb, int* a, uint32_t* n) {
@@ -431,10 +489,11 @@ __device__ __forceinline__ void decode(uint64_t k, int nb, int* a, uint32_t* n) 
 
 // One thread per sorted candidate: the SAH score of the first candidate of
 // each group of equal positions inside (cell_min + eps, cell_max - eps).
-__global__ void k_eval(const uint64_t* __restrict__ kc, size_t n_cand, size_t eTT, int nb,
+__global__ void k_eval(const uint64_t* __restrict__ kc, size_t n_cand, const unsigned long long* __restrict__ coff,
+                       const uint32_t* __restrict__ rb, uint32_t R, int nb,
                        const uint64_t* __restrict__ kmin, const uint64_t* __restrict__ kmax,
                        const uint64_t* __restrict__ kpl, size_t eGT, const uint32_t* __restrict__ grb,
-                       const uint32_t* __restrict__ ctb, const uint32_t* __restrict__ plb,
+                       const uint32_t* __restrict__ plb,
                        const uint32_t* __restrict__ pl_cnt, const NodeConst* __restrict__ nc, uint32_t N, Params P,
                        double* cost_out, uint8_t* side_out, unsigned long long* best_bits) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -468,7 +527,7 @@ __global__ void k_eval(const uint64_t* __restrict__ kc, size_t n_cand, size_t eT
     uint32_t n;
     decode(k, nb, &a, &n);
     const float p = key_pos(k);
-    const size_t s0 = (size_t)a * 2 * eTT + 2 * (size_t)ctb[n];
+    const size_t s0 = coff[(size_t)a * R + rb[n]];
     const NodeConst& c = nc[n];
     const bool head = (i == s0) || !(key_pos(kc[i - 1]) == p);
     if (head && p > c.lim_lo[a] && p < c.lim_hi[a]) {
@@ -544,18 +603,47 @@ __global__ void k_eval(const uint64_t* __restrict__ kc, size_t n_cand, size_t eT
     side_out[i] = side;
   }
   // min over the segment: a warp whose valid lanes share one segment
-  // reduces first and issues one atomic
+  // reduces first; a block whose warps all share one segment reduces again
+  // and issues one atomic (the top levels have three segments and tens of
+  // millions of candidates)
   unsigned long long bits = (unsigned long long)__double_as_longlong(cost);
   uint32_t lead = seg;
   for (int o = 16; o > 0; o >>= 1) lead = min(lead, __shfl_xor_sync(0xFFFFFFFFu, lead, o));
-  if (__all_sync(0xFFFFFFFFu, seg == lead || seg == kNone)) {
+  const bool warp_uniform = __all_sync(0xFFFFFFFFu, seg == lead || seg == kNone);
+  if (warp_uniform) {
     for (int o = 16; o > 0; o >>= 1) {
       const unsigned long long other = __shfl_xor_sync(0xFFFFFFFFu, bits, o);
       bits = other < bits ? other : bits;
     }
-    if ((threadIdx.x & 31) == 0 && lead != kNone) atomicMin(&best_bits[lead], bits);
   } else if (seg != kNone) {
     atomicMin(&best_bits[seg], bits);
+  }
+  __shared__ uint32_t s_seg[8];
+  __shared__ unsigned long long s_bits[8];
+  const int w = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_seg[w] = warp_uniform ? lead : 0xFFFFFFFEu;  // 0xFFFFFFFE: this warp has already issued its atomics
+    s_bits[w] = bits;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (int)(blockDim.x >> 5);
+    uint32_t bs = kNone;
+    bool same = true;
+    for (int k = 0; k < nw; ++k) {
+      if (s_seg[k] == kNone) continue;
+      if (s_seg[k] == 0xFFFFFFFEu || (bs != kNone && s_seg[k] != bs)) same = false;
+      if (bs == kNone && s_seg[k] != 0xFFFFFFFEu) bs = s_seg[k];
+    }
+    if (same && bs != kNone) {
+      unsigned long long m = ~0ull;
+      for (int k = 0; k < nw; ++k)
+        if (s_seg[k] == bs && s_bits[k] < m) m = s_bits[k];
+      atomicMin(&best_bits[bs], m);
+    } else {
+      for (int k = 0; k < nw; ++k)
+        if (s_seg[k] != kNone && s_seg[k] != 0xFFFFFFFEu) atomicMin(&best_bits[s_seg[k]], s_bits[k]);
+    }
   }
 }
 
@@ -891,9 +979,8 @@ int build_tree_gpu(const float* gauss, uint32_t n, const BuildParams& bp, HostTr
       exclusive_sum(S, flag.p, ridx.p, T + 1);
       const uint32_t R = read_one(S, ridx.p + T);
       DBuf<uint32_t> run_start(S, R + 1), run_node(S, R + 1), G(S, N + 1), rb(S, N + 1);
-      G.zero();
-      k_run_scatter<<<grid_for(T, 256), 256, 0, S.s>>>(flag.p, ridx.p, cur.node.p, T, run_start.p, run_node.p, G.p);
-      exclusive_sum(S, G.p, rb.p, N + 1);
+      k_run_scatter<<<grid_for(T, 256), 256, 0, S.s>>>(flag.p, ridx.p, cur.node.p, T, run_start.p, run_node.p);
+      k_node_runs<<<grid_for((size_t)N + 1, 128), 128, 0, S.s>>>(tb.p, ridx.p, N, rb.p, G.p);
       flag.release();
       ridx.release();
       // 2. node constants, eligible-node compaction
@@ -909,10 +996,16 @@ int build_tree_gpu(const float* gauss, uint32_t n, const BuildParams& bp, HostTr
       DBuf<uint32_t> is_split(S, N + 1);
       if (eTT > 0) {
         // 3. keys, sorts, scores
-        const size_t nc_keys = 6 * eTT;
+        DBuf<unsigned long long> ccnt(S, 3 * (size_t)R + 1), coff(S, 3 * (size_t)R + 1);
+        ccnt.zero();
+        k_run_cand_count<<<grid_for(R, 128), 128, 0, S.s>>>(run_start.p, run_node.p, R, T, cur.lo.p, cur.hi.p,
+                                                            cur.cap, nc.p, ccnt.p);
+        exclusive_sum(S, ccnt.p, coff.p, 3 * (size_t)R + 1);
+        ccnt.release();
+        const size_t nc_keys = read_one(S, coff.p + 3 * (size_t)R);
         DBuf<uint64_t> kc(S, nc_keys), kc_alt(S, nc_keys);
-        k_cand_keys<<<grid_for(T, 256), 256, 0, S.s>>>(cur.lo.p, cur.hi.p, cur.cap, T, cur.node.p, tb.p, nc.p,
-                                                       ctb.p, eTT, nb, kc.p);
+        k_run_cand_write<<<grid_for(R, 128), 128, 0, S.s>>>(run_start.p, run_node.p, R, T, cur.lo.p, cur.hi.p,
+                                                            cur.cap, nc.p, coff.p, nb, kc.p);
         DBuf<uint64_t> kmin(S, 3 * eGT), kmax(S, 3 * eGT), kpl(S, 3 * eGT), alt(S, 3 * eGT);
         DBuf<uint32_t> pl_cnt(S, 3 * (size_t)N + 1), plb(S, 3 * (size_t)N + 1);
         DBuf<unsigned long long> pl_fill(S, 1);
@@ -935,8 +1028,8 @@ int build_tree_gpu(const float* gauss, uint32_t n, const BuildParams& bp, HostTr
         DBuf<unsigned long long> best_bits(S, 3 * (size_t)N), best_idx(S, 3 * (size_t)N);
         best_bits.fill_ff();
         best_idx.fill_ff();
-        k_eval<<<grid_for(nc_keys, 256), 256, 0, S.s>>>(kc.p, nc_keys, eTT, nb, kmin.p, kmax.p, kpl.p, eGT, grb.p,
-                                                        ctb.p, plb.p, pl_cnt.p, nc.p, N, P, cost.p, side.p,
+        k_eval<<<grid_for(nc_keys, 256), 256, 0, S.s>>>(kc.p, nc_keys, coff.p, rb.p, R, nb, kmin.p, kmax.p, kpl.p,
+                                                        eGT, grb.p, plb.p, pl_cnt.p, nc.p, N, P, cost.p, side.p,
                                                         best_bits.p);
         k_argmin<<<grid_for(nc_keys, 256), 256, 0, S.s>>>(kc.p, cost.p, nc_keys, nb, N, best_bits.p, best_idx.p);
         k_choose<<<grid_for(N, 128), 128, 0, S.s>>>(nc.p, N, best_bits.p, best_idx.p, kc.p, side.p, dec.p,
