@@ -70,6 +70,7 @@ void kdgr_batch_config_default(kdgr_batch_config* c) {
   c->chunk = 1;
   c->precision = 0;
   c->hit_buffer = 4;
+  c->traversal = KDGR_TRAV_PACKET;
 }
 
 int kdgr_render_batch(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb, float* alpha, float* depth,
@@ -217,16 +218,19 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
   cudaEventCreate(&e1);
   std::string rep;
   float best_ms = 1e30f;
-  // stage 1: schedule x register cap x chunk with the 4-entry hit buffer;
-  // stage 2: the winner with the 8-entry buffer (dense leaves re-scan less)
+  // stage 1: schedule x register cap x chunk with warp packets and the
+  // 4-entry hit buffer; stage 2: the winner with the 8-entry buffer (dense
+  // leaves re-scan less) and the winner with per-ray traversal
   bool stage2 = false;
   for (size_t ci = 0; ci < cands.size() || !stage2; ++ci) {
-    if (ci == cands.size()) {  // reached once: appends the single stage-2 candidate
+    if (ci == cands.size()) {  // reached once: appends the stage-2 candidates
       stage2 = true;
       if (rc != KDGR_OK || best_ms >= 1e30f) break;
-      kdgr_batch_config c8 = *best;
+      kdgr_batch_config c8 = *best, cr = *best;
       c8.hit_buffer = 8;
+      cr.traversal = KDGR_TRAV_RAY;
       cands.push_back(c8);
+      cands.push_back(cr);
     }
     const kdgr_batch_config c = cands[ci];
     rc = run_once(s, c, table, totals, rgb, nullptr, nullptr, st, "kdgr_autotune");  // warm-up
@@ -247,8 +251,8 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
     char line[256];
     snprintf(line, sizeof(line),
              "{\"schedule\": %d, \"min_blocks\": %d, \"chunk\": %d, \"precision\": %d, \"hit_buffer\": %d, "
-             "\"ms\": %.4f}\n",
-             c.schedule, c.min_blocks, c.chunk, c.precision, c.hit_buffer, med);
+             "\"traversal\": %d, \"ms\": %.4f}\n",
+             c.schedule, c.min_blocks, c.chunk, c.precision, c.hit_buffer, c.traversal, med);
     rep += line;
     if (med < best_ms) {
       best_ms = med;

@@ -23,6 +23,9 @@
 //     (fma/mul/sub.rn.f32x2), half the arithmetic instructions per test;
 //   * the precision form reads a leaf's candidates kPipe at a time (all
 //     record loads in flight before the first test);
+//   * warp packets (the default traversal): the 32 rays of an 8x4 tile walk
+//     the tree together, each with its own interval and decisions, so a
+//     leaf's records are warp-uniform loads (pkt_trace below);
 //   * pixels are handed out in spatially coherent units (8x4 warp tiles,
 //     16x8 CTA blocks, or CTA blocks from per-SM contiguous strips) so the
 //     rays sharing an SM's L1 are neighbours; the autotuner picks the
@@ -495,6 +498,195 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
   return false;
 }
 
+// ------------------------------------------------------------ warp packets
+// Packet traversal of one 8x4 warp tile: the warp walks the tree together.
+// Primary rays of a tile share the eye point and, away from the image lines
+// where a direction component changes sign, the sign of every direction
+// component, so the front-to-back child order at a node is the same for all
+// of them.  Each lane keeps its own interval and makes the per-ray decision
+// of leaf_step (near child when t_split > t_near, far child when t_split <=
+// t_near or t_split < t_far); the warp enters a child when any lane needs it
+// and masks the others there.  A lane therefore meets exactly its own leaves,
+// in its own order, with its own [t_near, t_far), and the leaf's records are
+// warp-uniform loads.  Stack entries: (node, lane mask) per warp and
+// (t_near, t_far) per lane, a ring of kStack entries; when the ring has lost
+// entries the unfinished lanes restart at the root from the end of their
+// last leaf, as the per-ray short stack does.
+struct PktEnt {
+  uint32_t node, mask;
+};
+
+// Leaf [base, base + cnt) for the lanes with part set; every lane runs the
+// same candidate loop.  Returns false on a bad Gaussian ID (status set).
+template <int K, bool PACKED>
+__device__ __forceinline__ bool pkt_leaf(const FastView& S, uint32_t base, uint32_t cnt, Ray& R, bool part,
+                                         uint32_t* status) {
+  const float kInf = __int_as_float(0x7f800000);
+  bool have_last = false, ok = true;
+  float last_t = 0.f;
+  uint32_t last_i = 0;
+  bool more = part;
+  while (__any_sync(0xFFFFFFFFu, more)) {
+    HitBuf<K> hb;
+    hb.clear();
+    bool overflow = false;
+    const float tn = more ? R.t_near : kInf;
+    if constexpr (!PACKED) {
+      const uint32_t end = base + cnt;
+      const Ray2 w = ray2(R.o, R.d);
+      for (uint32_t e = base & ~1u; e < end; e += 2) {
+        const PairRec pr = load_pair(S, e >> 1);
+        float t2[2], g2[2];
+        unsigned m = test_pair(pr, w, tn, R.t_far, t2, g2);
+        if (e < base) m &= 2u;
+        if (e + 1 >= end) m &= 1u;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const uint32_t ik = e + k - base;
+          if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
+            overflow |= hb.insert(t2[k], g2[k], ik);
+        }
+      }
+    } else {
+      for (uint32_t i = 0; i < cnt; i += kPipe) {
+        Rec r[kPipe];
+#pragma unroll
+        for (int k = 0; k < kPipe; ++k) r[k] = load_rec(S, base + min(i + k, cnt - 1));
+#pragma unroll
+        for (int k = 0; k < kPipe; ++k) {
+          float t, g;
+          const uint32_t ik = i + k;
+          if (ik < cnt && test_rec(S, base + ik, r[k], R.o, R.d, tn, R.t_far, &t, &g) &&
+              (!have_last || t > last_t || (t == last_t && ik > last_i)))
+            overflow |= hb.insert(t, g, ik);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (hb.t[k] == kInf || R.A > 0.99f) break;
+      const uint32_t gid = __ldg(S.offsets + base + hb.i[k]);
+      if (gid >= S.n_gauss) {
+        atomicOr(status, kStatusBadId);
+        ok = false;
+        break;
+      }
+      const float gres = __expf(-0.0555555555556f * hb.g[k] * hb.g[k]);
+      const float alpha = fminf(0.99f, gauss_opacity<PACKED>(S, gid) * gres);
+      if (gres < 0.0113f || alpha < 1.0f / 255.0f) continue;
+      const F3 c = eval_sh_fast<PACKED>(S, gid, R.d);
+      const float w = alpha * (1.f - R.A);
+      R.r = fmaf(c.x, w, R.r);
+      R.g = fmaf(c.y, w, R.g);
+      R.b = fmaf(c.z, w, R.b);
+      R.D = fmaf(hb.t[k], w, R.D);
+      R.A += w;
+    }
+    more = more && ok && overflow && !(R.A > 0.99f);
+    have_last = true;
+    last_t = hb.t[K - 1];
+    last_i = hb.i[K - 1];
+  }
+  return ok;
+}
+
+// Trace the warp's rays as one packet.  live: the lane's ray entered the
+// scene box; sgn: bit a = sign of direction component a (warp-uniform).
+template <int K, bool PACKED>
+__device__ __forceinline__ void pkt_trace(const FastView& S, Ray& R, bool live, unsigned sgn,
+                                          uint32_t (*s_tn)[kThreads], float (*s_tf)[kThreads],
+                                          PktEnt (*s_ent)[kWarps], int tid, int warp, uint32_t* status) {
+  const unsigned full = 0xFFFFFFFFu;
+  bool act = live, done = !live;
+  float t_done = R.t_near;  // end of the part of the ray already composited
+  uint32_t cur = 0, steps = 0;
+  unsigned top = kStack - 1, quant = 0;
+  while (true) {
+    if (++steps > kMaxRaySteps) {
+      if ((tid & 31) == 0) atomicOr(status, kStatusStepLimit);
+      break;
+    }
+    uint2 nd = __ldg(S.nodes + cur);
+    bool leaf = true, bad = false;
+    while ((nd.x & 7u) != 3u) {
+      const uint32_t child = nd.x >> 3, axis = nd.x & 3u;
+      if (child + 1 >= S.n_nodes || ++steps > kMaxRaySteps) {
+        if ((tid & 31) == 0) atomicOr(status, child + 1 >= S.n_nodes ? kStatusBadNode : kStatusStepLimit);
+        bad = true;
+        break;
+      }
+      const unsigned sign = (sgn >> axis) & 1u;
+      const float t_split = (__uint_as_float(nd.y) - sel3(R.o, axis)) * sel3(R.inv, axis);
+      const bool wn = act && !(t_split <= R.t_near);
+      const bool wf = act && ((t_split <= R.t_near) || (t_split < R.t_far));
+      const unsigned bn = __ballot_sync(full, wn), bf = __ballot_sync(full, wf);
+      if (bn && bf) {
+        if (++top == kStack) top = 0;
+        quant = min(quant + 1, (unsigned)kStack);
+        s_ent[top][warp] = PktEnt{child + (sign ^ 1u), bf};
+        s_tn[top][tid] = __float_as_uint(wn ? t_split : R.t_near);
+        s_tf[top][tid] = R.t_far;
+        if (wn && wf) R.t_far = t_split;
+        act = wn;
+        cur = child + sign;
+      } else if (bn) {
+        cur = child + sign;
+      } else if (bf) {
+        cur = child + (sign ^ 1u);
+      } else {
+        leaf = false;
+        break;
+      }
+      nd = __ldg(S.nodes + cur);
+    }
+    if (bad) break;
+    if (leaf) {
+      const uint32_t cnt = nd.x >> 3, base = nd.y;
+      if ((uint64_t)base + cnt > S.n_offsets) {
+        if ((tid & 31) == 0) atomicOr(status, kStatusBadLeaf);
+        break;
+      }
+      const bool part = act && !done;
+      if (__any_sync(full, part)) {
+        if (!pkt_leaf<K, PACKED>(S, base, cnt, R, part, status)) done = true;
+        if (part) {
+          t_done = R.t_far;
+          if (R.A > 0.99f || R.t_far >= R.t_scene_far) done = true;
+        }
+      }
+    }
+    // next subtree: pop entries until one holds an unfinished lane
+    bool found = false;
+    while (quant > 0) {
+      const PktEnt e = s_ent[top][warp];
+      const float tn = __uint_as_float(s_tn[top][tid]), tf = s_tf[top][tid];
+      if (top == 0) top = kStack;
+      --top;
+      --quant;
+      act = ((e.mask >> (tid & 31)) & 1u) && !done;
+      if (act) {
+        R.t_near = tn;
+        R.t_far = tf;
+      }
+      if (__any_sync(full, act)) {
+        cur = e.node;
+        found = true;
+        break;
+      }
+    }
+    if (!found) {
+      // the ring lost entries: unfinished lanes restart at the root
+      act = !done;
+      if (!__any_sync(full, act)) break;
+      cur = 0;
+      if (act) {
+        R.t_near = t_done;
+        R.t_far = R.t_scene_far;
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ int find_view(const ViewDesc* views, int n_views, uint32_t item, int sched) {
   int lo = 0, hi = n_views - 1;
   while (lo < hi) {
@@ -506,18 +698,10 @@ __device__ __forceinline__ int find_view(const ViewDesc* views, int n_views, uin
   return lo;
 }
 
-// Render the ray of pixel (x, y) of view V to completion and store it.
-template <int K, bool PACKED>
-__device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, int x, int y,
-                                          uint32_t (*s_id)[kThreads], float (*s_t)[kThreads], int tid, float* rgb,
-                                          float* alpha_out, float* depth_out, uint32_t* status) {
+// Store the ray of pixel (x, y) of view V.
+__device__ __forceinline__ void store_px(const ViewDesc& V, int x, int y, const Ray& R, float* rgb, float* alpha_out,
+                                         float* depth_out) {
   const int W = __ldg(&V.W), H = __ldg(&V.H);
-  if (x >= W || y >= H) return;
-  Ray R;
-  if (ray_init(S, V.cam, x, y, R)) {
-    while (R.A < 0.99f && !leaf_step<K, PACKED>(S, s_id, s_t, tid, R, status)) {
-    }
-  }
   const size_t idx = (size_t)__ldg(&V.out_off) + (size_t)(H - 1 - y) * W + x;  // rows flipped per view
   rgb[3 * idx] = R.r;
   rgb[3 * idx + 1] = R.g;
@@ -526,13 +710,50 @@ __device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, 
   if (depth_out) depth_out[idx] = R.D;
 }
 
+// Render the ray of pixel (x, y) of view V to completion and store it.
+// PKT: warp packets (every lane of the warp calls this together); otherwise
+// one independent ray per lane.
+template <int K, bool PACKED, bool PKT>
+__device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, int x, int y,
+                                          uint32_t (*s_id)[kThreads], float (*s_t)[kThreads],
+                                          PktEnt (*s_ent)[kWarps], int tid, float* rgb, float* alpha_out,
+                                          float* depth_out, uint32_t* status) {
+  const int W = __ldg(&V.W), H = __ldg(&V.H);
+  if constexpr (PKT) {
+    const bool inimg = x < W && y < H;
+    Ray R;
+    const bool live = ray_init(S, V.cam, inimg ? x : 0, inimg ? y : 0, R) && inimg;
+    // one packet per direction-sign pattern among the warp's rays (almost
+    // always one; two or more only for tiles on a sign-change line)
+    const unsigned my_sgn = (__float_as_uint(R.inv.x) >> 31) | ((__float_as_uint(R.inv.y) >> 31) << 1) |
+                            ((__float_as_uint(R.inv.z) >> 31) << 2);
+    unsigned pending = __ballot_sync(0xFFFFFFFFu, live);
+    while (pending) {
+      const unsigned sgn = __shfl_sync(0xFFFFFFFFu, my_sgn, __ffs(pending) - 1);
+      const bool in = live && my_sgn == sgn && ((pending >> (tid & 31)) & 1u);
+      pending &= ~__ballot_sync(0xFFFFFFFFu, in);
+      pkt_trace<K, PACKED>(S, R, in, sgn, s_id, s_t, s_ent, tid, tid >> 5, status);
+    }
+    if (!inimg) return;
+    store_px(V, x, y, R, rgb, alpha_out, depth_out);
+  } else {
+    if (x >= W || y >= H) return;
+    Ray R;
+    if (ray_init(S, V.cam, x, y, R)) {
+      while (R.A < 0.99f && !leaf_step<K, PACKED>(S, s_id, s_t, tid, R, status)) {
+      }
+    }
+    store_px(V, x, y, R, rgb, alpha_out, depth_out);
+  }
+}
+
 // Persistent kernel.  Schedules (include/kdgr.h):
 //   WARP_TILES: each warp takes `chunk` 8x4 tiles from the global queue;
 //   CTA_BLOCKS: each CTA takes `chunk` 16x8 blocks (barrier per block) and
 //               its four warps render the four quarters, so the rays sharing
 //               the SM's L1 are neighbours.
 // MINB caps registers so that MINB CTAs fit per SM (0: compiler's choice).
-template <bool PACKED, int SCHED, int MINB, int KB>
+template <bool PACKED, int SCHED, int MINB, int KB, bool PKT>
 __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, const ViewDesc* __restrict__ views,
                                                                  int n_views, uint32_t total_items,
                                                                  float* __restrict__ rgb,
@@ -541,6 +762,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
                                                                  uint32_t* status, int chunk) {
   __shared__ uint32_t s_id[kStack][kThreads];
   __shared__ float s_t[kStack][kThreads];
+  __shared__ PktEnt s_ent[kStack][kWarps];
   __shared__ uint32_t s_work;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if constexpr (SCHED == KDGR_SCHED_SM_STRIPS) {
@@ -570,7 +792,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
       const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
       const int x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
       const int y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
-      render_px<KB, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
+      render_px<KB, PACKED, PKT>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
     }
   } else {
     while (true) {
@@ -599,7 +821,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
           x = (int)(lt % nx) * kTileW + (lane & 7);
           y = (int)(lt / nx) * kTileH + (lane >> 3);
         }
-        render_px<KB, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, alpha_out, depth_out, status);
+        render_px<KB, PACKED, PKT>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
       }
     }
   }
@@ -616,6 +838,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_render_multi(const FastView* __
                                                               uint32_t* queue, uint32_t* status) {
   __shared__ uint32_t s_id[kStack][kThreads];
   __shared__ float s_t[kStack][kThreads];
+  __shared__ PktEnt s_ent[kStack][kWarps];
   __shared__ uint32_t s_work;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   while (true) {
@@ -629,7 +852,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_render_multi(const FastView* __
     const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
     const int x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
     const int y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
-    render_px<kHits, PACKED>(S, V, x, y, s_id, s_t, tid, rgb, nullptr, nullptr, status);
+    render_px<kHits, PACKED, true>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, nullptr, nullptr, status);
   }
 }
 
@@ -662,23 +885,28 @@ __global__ void k_aniso_fp64(const float* __restrict__ src, uint32_t n, float4* 
 using KernelFn = void (*)(FastView, const ViewDesc*, int, uint32_t, float*, float*, float*, uint32_t*, uint32_t*,
                           int);
 
-template <bool PACKED, int SCHED, int KB>
+template <bool PACKED, int SCHED, int KB, bool PKT>
 KernelFn pick_minb(int minb) {
-  if (minb >= 8) return k_render_batch<PACKED, SCHED, 8, KB>;
-  if (minb >= 6) return k_render_batch<PACKED, SCHED, 6, KB>;
-  return k_render_batch<PACKED, SCHED, 0, KB>;
+  if (minb >= 8) return k_render_batch<PACKED, SCHED, 8, KB, PKT>;
+  if (minb >= 6) return k_render_batch<PACKED, SCHED, 6, KB, PKT>;
+  return k_render_batch<PACKED, SCHED, 0, KB, PKT>;
 }
 
-template <bool PACKED, int KB>
+template <bool PACKED, int KB, bool PKT>
 KernelFn pick_sched_k(const kdgr_batch_config& c) {
-  if (c.schedule == KDGR_SCHED_CTA_BLOCKS) return pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS, KB>(c.min_blocks);
-  if (c.schedule == KDGR_SCHED_SM_STRIPS) return pick_minb<PACKED, KDGR_SCHED_SM_STRIPS, KB>(c.min_blocks);
-  return pick_minb<PACKED, KDGR_SCHED_WARP_TILES, KB>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_CTA_BLOCKS) return pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS, KB, PKT>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_SM_STRIPS) return pick_minb<PACKED, KDGR_SCHED_SM_STRIPS, KB, PKT>(c.min_blocks);
+  return pick_minb<PACKED, KDGR_SCHED_WARP_TILES, KB, PKT>(c.min_blocks);
+}
+
+template <bool PACKED, bool PKT>
+KernelFn pick_sched_t(const kdgr_batch_config& c) {
+  return c.hit_buffer == 8 ? pick_sched_k<PACKED, 8, PKT>(c) : pick_sched_k<PACKED, kHits, PKT>(c);
 }
 
 template <bool PACKED>
 KernelFn pick_sched(const kdgr_batch_config& c) {
-  return c.hit_buffer == 8 ? pick_sched_k<PACKED, 8>(c) : pick_sched_k<PACKED, kHits>(c);
+  return c.traversal == KDGR_TRAV_RAY ? pick_sched_t<PACKED, false>(c) : pick_sched_t<PACKED, true>(c);
 }
 
 KernelFn pick_kernel(const kdgr_batch_config& c) {
@@ -791,6 +1019,10 @@ int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
   }
   if (c.min_blocks != 0 && c.min_blocks != 6 && c.min_blocks != 8) {
     set_error("batch config: min_blocks must be 0, 6 or 8");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (c.traversal != KDGR_TRAV_PACKET && c.traversal != KDGR_TRAV_RAY) {
+    set_error("batch config: traversal must be KDGR_TRAV_PACKET or KDGR_TRAV_RAY");
     return KDGR_ERR_INVALID_ARG;
   }
   return KDGR_OK;

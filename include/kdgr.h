@@ -216,6 +216,12 @@ typedef struct {
                                     SM; a CTA takes the next block of its SM's strip (neighbours share
                                     the SM's L1) and steals from the following strips when it is done */
 
+/* Tree walk of the batch kernel.  Both give every ray its own leaves, in its
+ * own front-to-back order, with its own leaf intervals. */
+#define KDGR_TRAV_PACKET 0 /* the 32 rays of a warp's 8x4 tile walk the tree together (a child is entered
+                              when any ray needs it); leaf records become warp-uniform loads */
+#define KDGR_TRAV_RAY 1    /* each lane walks its own ray independently */
+
 typedef struct {
   int32_t schedule;      /* KDGR_SCHED_* */
   int32_t min_blocks;    /* register cap: 0 (compiler), 6 or 8 resident 128-thread CTAs per SM */
@@ -224,6 +230,7 @@ typedef struct {
   int32_t precision;     /* 0: FP32 arrays (KDGR_FORM_FAST); 1: BF16/FP16 arrays (KDGR_FORM_PACKED) */
   int32_t hit_buffer;    /* per-leaf register hit buffer: 4 or 8 entries (0 = 4); a leaf with more
                             accepted hits is re-scanned for the next ones */
+  int32_t traversal;     /* KDGR_TRAV_*: how the rays of a warp walk the tree */
 } kdgr_batch_config;
 
 void kdgr_batch_config_default(kdgr_batch_config* cfg);

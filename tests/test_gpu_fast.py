@@ -84,7 +84,8 @@ def test_batch_equals_single_views_and_graph(pkg, cuda, fixtures):
 
 def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     """Warp tiles, CTA blocks and SM strips (with several chunk sizes and
-    register caps) only change which lane renders which pixel."""
+    register caps) only change which lane renders which pixel; warp packets
+    and per-ray traversal give every ray the same leaves and intervals."""
     fx = fixtures["cluster2k"]
     F = pkg.renderer
     scene = F.Scene(fx.tree, fx.rec)
@@ -93,15 +94,16 @@ def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     ref = torch.zeros(total * 3, device=cuda)
     ref_a = torch.zeros(total, device=cuda)
     scene.render_batch(views, len(cams), ref, ref_a)
-    for sched, chunk, minb, kb in [(0, 1, 0, 4), (0, 3, 8, 8), (0, 7, 6, 4), (1, 1, 6, 8), (1, 2, 0, 4),
-                                   (1, 5, 8, 4), (2, 1, 0, 8), (2, 1, 8, 4)]:
-        cfg = F.BatchConfig(sched, minb, 0, chunk, 0, kb)
+    for sched, chunk, minb, kb, trav in [(0, 1, 0, 4, 0), (0, 3, 8, 8, 0), (0, 7, 6, 4, 1), (1, 1, 6, 8, 0),
+                                         (1, 2, 0, 4, 1), (1, 5, 8, 4, 0), (2, 1, 0, 8, 1), (2, 1, 8, 4, 0),
+                                         (1, 1, 8, 4, 1), (2, 1, 8, 8, 1)]:
+        cfg = F.BatchConfig(sched, minb, 0, chunk, 0, kb, trav)
         out = torch.full_like(ref, -1.0)
         out_a = torch.full_like(ref_a, -1.0)
         scene.render_batch(views, len(cams), out, out_a, cfg=cfg)
         torch.cuda.synchronize()
-        assert float((out - ref).abs().max()) <= 1e-5, (sched, chunk, minb)
-        assert float((out_a - ref_a).abs().max()) <= 1e-5, (sched, chunk, minb)
+        assert float((out - ref).abs().max()) <= 1e-5, (sched, chunk, minb, trav)
+        assert float((out_a - ref_a).abs().max()) <= 1e-5, (sched, chunk, minb, trav)
     scene.close()
 
 
@@ -114,8 +116,8 @@ def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
     rgb = torch.zeros(total * 3, device=cuda)
     best, report = scene.autotune(views, len(cams), rgb)
     assert best.schedule in (0, 1, 2) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
-    assert len(report.strip().splitlines()) == 16
-    assert best.hit_buffer in (4, 8)
+    assert len(report.strip().splitlines()) == 17
+    assert best.hit_buffer in (4, 8) and best.traversal in (F.TRAV_PACKET, F.TRAV_RAY)
     ref = torch.zeros_like(rgb)
     scene.render_batch(views, len(cams), ref)
     out = torch.zeros_like(rgb)
@@ -153,7 +155,8 @@ def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
     deeper than the ring (restarts), 20 equal-t hits in one leaf (more than
     the hit buffer: re-scan passes), a 100-candidate leaf, a Gaussian across
     a split, an empty scene and a missed box; both within the accuracy bar
-    of the FP64 oracle, and the FP32 form equal across every schedule."""
+    of the FP64 oracle, and the FP32 form equal across every schedule and
+    both traversals."""
     import kat
     (tree, rec, cam), W, H = KAT_CASES[case](kat)
     F = pkg.renderer
@@ -166,9 +169,9 @@ def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
     views, total, _ = F.make_views([(cam, W, H)])
     ref = torch.zeros(total * 3, device=cuda)
     scene.render_batch(views, 1, ref)
-    for sched, kb in [(0, 4), (1, 8), (2, 4)]:
+    for sched, kb, trav in [(0, 4, 0), (1, 8, 0), (2, 4, 0), (0, 4, 1), (1, 8, 1)]:
         out = torch.full_like(ref, -1.0)
-        scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, 0, kb))
+        scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, 0, kb, trav))
         torch.cuda.synchronize()
         np.testing.assert_array_equal(out.cpu().numpy(), ref.cpu().numpy())
     assert scene.status() == 0
