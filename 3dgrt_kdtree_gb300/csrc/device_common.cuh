@@ -38,8 +38,12 @@ struct ExactView {
 // Device arrays of the fast forms.
 //   nodes:      re-laid-out tree: the top levels breadth-first, the rest
 //               depth-first by subtree; children stay pairwise adjacent.
-//               Leaf words are unchanged.
-//   offsets:    leaf Gaussian-ID lists (read for accepted hits only);
+//               Leaf words: x as in the file (count << 3 | 3), y = the
+//               leaf's first pair p; its entries are 2p .. 2p + count - 1,
+//               and an odd leaf ends with one padding entry;
+//   offsets:    Gaussian ID of every entry in that padded leaf order
+//               (0xFFFFFFFF for padding), read for accepted hits only;
+//               n_offsets counts the padded entries;
 //   opacity:    1 float per Gaussian;
 //   sh:         FP32 coefficient-major (shared with ExactView);
 //   sh_bf16:    6 x uint4 per Gaussian, BF16 coefficient-major;
@@ -50,6 +54,8 @@ struct ExactView {
 //               M = diag(1/s) R^T and b = M mu interleaved lo/hi, 6 x float4;
 //   leaf_packed: packed form, per leaf entry 2 x uint4: (mu.xyz f32, half2
 //               (M22, flag)) and the other eight entries of M as four half2.
+//   Padding entries hold zero records: M = 0 gives |grdu|^2 = 0 and
+//   t* = 0 * inf = NaN, which no leaf interval accepts.
 struct FastView {
   const uint2* nodes;
   const uint32_t* offsets;

@@ -109,6 +109,18 @@ void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std:
   }
 }
 
+void pad_leaf_pairs(std::vector<uint32_t>& relaid, const uint32_t* offsets, std::vector<uint32_t>& pair_gid) {
+  pair_gid.clear();
+  for (size_t n = 0; 2 * n < relaid.size(); ++n) {
+    const uint32_t x = relaid[2 * n];
+    if ((x & 7u) != 3u) continue;
+    const uint32_t cnt = x >> 3, off = relaid[2 * n + 1];
+    relaid[2 * n + 1] = (uint32_t)(pair_gid.size() / 2);
+    pair_gid.insert(pair_gid.end(), offsets + off, offsets + off + cnt);
+    if (cnt & 1u) pair_gid.push_back(kPadGid);
+  }
+}
+
 }  // namespace kdgr
 
 using namespace kdgr;
@@ -132,7 +144,7 @@ kdgr::ExactView kdgr_scene_s::exact_view() const {
 kdgr::FastView kdgr_scene_s::fast_view() const {
   FastView v;
   v.nodes = d_nodes_fast;
-  v.offsets = d_offsets;
+  v.offsets = d_pair_gid;
   v.opacity = d_opacity;
   v.sh = d_sh;
   v.sh_bf16 = d_sh_bf16;
@@ -141,7 +153,7 @@ kdgr::FastView kdgr_scene_s::fast_view() const {
   v.leaf_pairs = d_leaf_pairs;
   v.leaf_packed = d_leaf_packed;
   v.n_nodes = n_nodes;
-  v.n_offsets = n_offsets;
+  v.n_offsets = n_pair_entries;
   v.n_gauss = n_gauss;
   v.top_nodes = top_nodes;
   for (int i = 0; i < 3; ++i) {
@@ -280,11 +292,21 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
       return fail("kdgr_scene_create: upload (exact)");
   }
   if (forms & (KDGR_FORM_FAST | KDGR_FORM_PACKED)) {
-    std::vector<uint32_t> relaid;
+    std::vector<uint32_t> relaid, pair_gid;
     relayout_tree(nodes, n_nodes, kTopLevels, relaid, &s->top_nodes);
+    pad_leaf_pairs(relaid, offsets, pair_gid);
+    if (pair_gid.size() > 0xFFFFFFF0ull) {
+      A.release();
+      set_error("kdgr_scene_create: more than 2^32 leaf entries after pair padding");
+      return KDGR_ERR_LIMIT;
+    }
+    s->n_pair_entries = (uint32_t)pair_gid.size();
     s->d_nodes_fast = A.alloc<uint2>(n_nodes);
+    s->d_pair_gid = A.alloc<uint32_t>(pair_gid.size() + 2);
     if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (tree)");
-    if (cudaMemcpy(s->d_nodes_fast, relaid.data(), 8ull * n_nodes, cudaMemcpyHostToDevice) != cudaSuccess)
+    if (cudaMemcpy(s->d_nodes_fast, relaid.data(), 8ull * n_nodes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (!pair_gid.empty() && cudaMemcpy(s->d_pair_gid, pair_gid.data(), 4 * pair_gid.size(),
+                                         cudaMemcpyHostToDevice) != cudaSuccess))
       return fail("kdgr_scene_create: upload (tree)");
   }
   if (forms & KDGR_FORM_FAST) {
@@ -308,14 +330,14 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
       op[i] = r[3];
     }
     s->d_opacity = A.alloc<float>(n);
-    s->d_leaf_pairs = A.alloc<float4>(6 * (((size_t)n_offsets + 1) / 2 + 1));
+    s->d_leaf_pairs = A.alloc<float4>(6 * ((size_t)s->n_pair_entries / 2 + 1));
     if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (fast)");
     // the per-Gaussian records are staging only: the kernels read the leaf-order pairs
     float4* d_stage = nullptr;
     cudaError_t e = cudaMalloc(&d_stage, tf.size() * 4);
     if (e == cudaSuccess) e = cudaMemcpy(d_stage, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(s->d_opacity, op.data(), op.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = build_leaf_pairs(s->d_offsets, n_offsets, d_stage, s->d_leaf_pairs);
+    if (e == cudaSuccess) e = build_leaf_pairs(s->d_pair_gid, s->n_pair_entries, d_stage, s->d_leaf_pairs);
     if (d_stage) cudaFree(d_stage);
     if (e != cudaSuccess) return fail("kdgr_scene_create: upload (fast)");
   }
@@ -336,7 +358,7 @@ int kdgr_scene_destroy(kdgr_scene_t s) {
   if (!s) return KDGR_ERR_INVALID_ARG;
   void* ps[] = {s->d_nodes,     s->d_offsets, s->d_test,      s->d_sh,          s->d_nodes_fast,
                 s->d_opacity,   s->d_sh_bf16,     s->d_aniso_idx,
-                s->d_aniso,     s->d_leaf_pairs, s->d_leaf_packed, s->d_status};
+                s->d_aniso,     s->d_leaf_pairs, s->d_leaf_packed, s->d_pair_gid, s->d_status};
   cudaError_t first = cudaSuccess;
   for (void* p : ps)
     if (p) {

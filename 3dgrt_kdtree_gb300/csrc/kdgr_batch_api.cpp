@@ -64,8 +64,10 @@ extern "C" {
 
 void kdgr_batch_config_default(kdgr_batch_config* c) {
   if (!c) return;
-  c->schedule = KDGR_SCHED_CTA_BLOCKS;
-  c->min_blocks = 8;  // 64 registers, 8 CTAs per SM: the fastest variant measured on GB300
+  // SM strips, 64 registers (8 CTAs per SM), warp packets: the autotuner's
+  // pick on GB300 for one 1080p view, 64 mixed views and the 3M scene
+  c->schedule = KDGR_SCHED_SM_STRIPS;
+  c->min_blocks = 8;
   c->blocks_per_sm = 0;
   c->chunk = 1;
   c->precision = 0;
@@ -200,9 +202,10 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
   if (rc != KDGR_OK) return rc;
   std::vector<kdgr_batch_config> cands;
   for (int minb : {0, 6, 8})
-    for (int sched : {KDGR_SCHED_WARP_TILES, KDGR_SCHED_CTA_BLOCKS, KDGR_SCHED_SM_STRIPS})
+    for (int sched : {KDGR_SCHED_WARP_TILES, KDGR_SCHED_CTA_BLOCKS, KDGR_SCHED_SM_STRIPS, KDGR_SCHED_WARP_STRIPS})
       for (int chunk : {1, 2}) {
-        if (sched == KDGR_SCHED_SM_STRIPS && chunk != 1) continue;  // strips take one block per claim
+        // strips take one item per claim
+        if ((sched == KDGR_SCHED_SM_STRIPS || sched == KDGR_SCHED_WARP_STRIPS) && chunk != 1) continue;
         kdgr_batch_config c = base;
         c.min_blocks = minb;
         c.schedule = sched;

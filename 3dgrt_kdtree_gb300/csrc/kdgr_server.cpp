@@ -283,8 +283,9 @@ void kdgr_server_s::completer() {
 
 static uint64_t estimate_scene_bytes(uint32_t n_nodes, uint32_t n_offsets, uint32_t n, bool packed) {
   const uint64_t per = packed ? (96 + 4 + 4) : (4 + 192);  // SH, opacity (+ aniso index)
-  const uint64_t per_entry = 4 + (packed ? 32 : 48);  // ID + leaf-order record
-  return 8ull * n_nodes + per_entry * n_offsets + per * n;
+  // ID, padded-order ID and leaf-order record; each leaf may add one padding entry
+  const uint64_t per_entry = 8 + (packed ? 32 : 48);
+  return 16ull * n_nodes + per_entry * (n_offsets + n_nodes / 2 + 1) + per * n;
 }
 
 extern "C" {

@@ -236,6 +236,45 @@ __device__ __forceinline__ unsigned test_pair(const PairRec& r, const Ray2& w, f
   return m;
 }
 
+// test_pair in two steps for warp packets, so the warp can skip the second
+// step (and the hit insertion) together when no lane's t* is in range.
+struct PairT {
+  f2 ng[3], gd[3];
+  float r0, r1;
+};
+__device__ __forceinline__ unsigned test_pair_t(const PairRec& r, const Ray2& w, float t_near, float t_far, float t[2],
+                                                PairT& p) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const f2 m0 = r.q[2 * i].x, m1 = r.q[2 * i].y, m2 = r.q[2 * i + 1].x, b = r.q[2 * i + 1].y;
+    p.ng[i] = fma2(m0, w.nox, fma2(m1, w.noy, fma2(m2, w.noz, b)));
+    p.gd[i] = fma2(m0, w.dx, fma2(m1, w.dy, mul2(m2, w.dz)));
+  }
+  const f2 q = fma2(p.gd[0], p.gd[0], fma2(p.gd[1], p.gd[1], mul2(p.gd[2], p.gd[2])));
+  const f2 a = fma2(p.gd[0], p.ng[0], fma2(p.gd[1], p.ng[1], mul2(p.gd[2], p.ng[2])));
+  float q0, q1, a0, a1;
+  split2(q, q0, q1);
+  split2(a, a0, a1);
+  p.r0 = __fdividef(1.f, q0);
+  p.r1 = __fdividef(1.f, q1);
+  t[0] = a0 * p.r0;
+  t[1] = a1 * p.r1;
+  return ((t[0] >= t_near && t[0] < t_far) ? 1u : 0u) | ((t[1] >= t_near && t[1] < t_far) ? 2u : 0u);
+}
+__device__ __forceinline__ unsigned test_pair_g(const PairT& p, unsigned m, float g[2]) {
+  const f2 c0 = sub2(mul2(p.gd[1], p.ng[2]), mul2(p.gd[2], p.ng[1]));
+  const f2 c1 = sub2(mul2(p.gd[2], p.ng[0]), mul2(p.gd[0], p.ng[2]));
+  const f2 c2 = sub2(mul2(p.gd[0], p.ng[1]), mul2(p.gd[1], p.ng[0]));
+  const f2 cc = fma2(c0, c0, fma2(c1, c1, mul2(c2, c2)));
+  float cc0, cc1;
+  split2(cc, cc0, cc1);
+  g[0] = cc0 * p.r0;
+  g[1] = cc1 * p.r1;
+  if (!(g[0] < 8.f)) m &= ~1u;
+  if (!(g[1] < 8.f)) m &= ~2u;
+  return m;
+}
+
 template <bool PACKED>
 __device__ __forceinline__ float gauss_opacity(const FastView& S, uint32_t gid) {
   return __ldg(S.opacity + gid);
@@ -405,14 +444,10 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
       s_t[R.top][tid] = R.t_far;
       R.t_far = t_split;
     }
-    if (child + 1 >= S.n_nodes || ++R.steps > kMaxRaySteps) {
-      atomicOr(status, child + 1 >= S.n_nodes ? kStatusBadNode : kStatusStepLimit);
-      return true;
-    }
     R.cur = idx;
     nd = __ldg(S.nodes + R.cur);
   }
-  const uint32_t cnt = nd.x >> 3, base = nd.y;
+  const uint32_t cnt = nd.x >> 3, pb = nd.y, base = 2 * pb;  // first pair, first entry
   if ((uint64_t)base + cnt > S.n_offsets) {
     atomicOr(status, kStatusBadLeaf);
     return true;
@@ -425,17 +460,15 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     hb.clear();
     bool overflow = false;
     if constexpr (!PACKED) {
-      const uint32_t end = base + cnt;
+      const uint32_t np = (cnt + 1) >> 1;
       const Ray2 w = ray2(R.o, R.d);
-      for (uint32_t e = base & ~1u; e < end; e += 2) {
-        const PairRec pr = load_pair(S, e >> 1);
+      for (uint32_t p = 0; p < np; ++p) {
+        const PairRec pr = load_pair(S, pb + p);
         float t2[2], g2[2];
-        unsigned m = test_pair(pr, w, R.t_near, R.t_far, t2, g2);
-        if (e < base) m &= 2u;     // low half belongs to the previous leaf
-        if (e + 1 >= end) m &= 1u;  // high half belongs to the next leaf
+        const unsigned m = test_pair(pr, w, R.t_near, R.t_far, t2, g2);  // padding: NaN t*, never passes
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-          const uint32_t ik = e + k - base;
+          const uint32_t ik = 2 * p + k;
           if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
             overflow |= hb.insert(t2[k], g2[k], ik);
         }
@@ -526,25 +559,31 @@ __device__ __forceinline__ bool pkt_leaf(const FastView& S, uint32_t base, uint3
   float last_t = 0.f;
   uint32_t last_i = 0;
   bool more = part;
+  const uint32_t pb = base >> 1;
   while (__any_sync(0xFFFFFFFFu, more)) {
     HitBuf<K> hb;
     hb.clear();
     bool overflow = false;
     const float tn = more ? R.t_near : kInf;
     if constexpr (!PACKED) {
-      const uint32_t end = base + cnt;
+      const uint32_t np = (cnt + 1) >> 1;
       const Ray2 w = ray2(R.o, R.d);
-      for (uint32_t e = base & ~1u; e < end; e += 2) {
-        const PairRec pr = load_pair(S, e >> 1);
+      for (uint32_t p = 0; p < np; ++p) {
+        const PairRec pr = load_pair(S, pb + p);
         float t2[2], g2[2];
-        unsigned m = test_pair(pr, w, tn, R.t_far, t2, g2);
-        if (e < base) m &= 2u;
-        if (e + 1 >= end) m &= 1u;
+        PairT pt;
+        unsigned m = test_pair_t(pr, w, tn, R.t_far, t2, pt);  // padding: NaN t*, never passes
+        // warp-uniform branches: most pairs have no lane with t* in range
+        if (__any_sync(0xFFFFFFFFu, m != 0u)) {
+          m = test_pair_g(pt, m, g2);
+          if (__any_sync(0xFFFFFFFFu, m != 0u)) {
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const uint32_t ik = e + k - base;
-          if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
-            overflow |= hb.insert(t2[k], g2[k], ik);
+            for (int k = 0; k < 2; ++k) {
+              const uint32_t ik = 2 * p + k;
+              if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
+                overflow |= hb.insert(t2[k], g2[k], ik);
+            }
+          }
         }
       }
     } else {
@@ -607,14 +646,9 @@ __device__ __forceinline__ void pkt_trace(const FastView& S, Ray& R, bool live, 
       break;
     }
     uint2 nd = __ldg(S.nodes + cur);
-    bool leaf = true, bad = false;
+    bool leaf = true;
     while ((nd.x & 7u) != 3u) {
       const uint32_t child = nd.x >> 3, axis = nd.x & 3u;
-      if (child + 1 >= S.n_nodes || ++steps > kMaxRaySteps) {
-        if ((tid & 31) == 0) atomicOr(status, child + 1 >= S.n_nodes ? kStatusBadNode : kStatusStepLimit);
-        bad = true;
-        break;
-      }
       const unsigned sign = (sgn >> axis) & 1u;
       const float t_split = (__uint_as_float(nd.y) - sel3(R.o, axis)) * sel3(R.inv, axis);
       const bool wn = act && !(t_split <= R.t_near);
@@ -639,9 +673,8 @@ __device__ __forceinline__ void pkt_trace(const FastView& S, Ray& R, bool live, 
       }
       nd = __ldg(S.nodes + cur);
     }
-    if (bad) break;
     if (leaf) {
-      const uint32_t cnt = nd.x >> 3, base = nd.y;
+      const uint32_t cnt = nd.x >> 3, base = 2 * nd.y;  // first entry of the leaf's first pair
       if ((uint64_t)base + cnt > S.n_offsets) {
         if ((tid & 31) == 0) atomicOr(status, kStatusBadLeaf);
         break;
@@ -749,6 +782,9 @@ __device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, 
 
 // Persistent kernel.  Schedules (include/kdgr.h):
 //   WARP_TILES: each warp takes `chunk` 8x4 tiles from the global queue;
+//   WARP_STRIPS: each warp takes the next 8x4 tile (in 16x8-block order) of
+//               its SM's strip of the block list, then steals from the
+//               following strips;
 //   CTA_BLOCKS: each CTA takes `chunk` 16x8 blocks (barrier per block) and
 //               its four warps render the four quarters, so the rays sharing
 //               the SM's L1 are neighbours.
@@ -765,7 +801,31 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
   __shared__ PktEnt s_ent[kStack][kWarps];
   __shared__ uint32_t s_work;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if constexpr (SCHED == KDGR_SCHED_SM_STRIPS) {
+  if constexpr (SCHED == KDGR_SCHED_WARP_STRIPS) {
+    // items are quarters of 16x8 blocks (8x4 tiles in block order); each
+    // warp claims the next quarter of its SM's strip, no CTA barrier
+    uint32_t smid;
+    asm("mov.u32 %0, %%smid;" : "=r"(smid));
+    const uint32_t n = (uint32_t)chunk;  // number of strips
+    uint32_t k = smid % n, visited = 0;
+    while (visited < n) {
+      const uint32_t b0 = (uint32_t)((uint64_t)total_items * k / n), b1 = (uint32_t)((uint64_t)total_items * (k + 1) / n);
+      uint32_t it = 0;
+      if (lane == 0) it = b0 + atomicAdd(queue + 1 + k, 1u);
+      it = __shfl_sync(0xFFFFFFFFu, it, 0);
+      if (it >= b1) {
+        k = (k + 1) % n;
+        ++visited;
+        continue;
+      }
+      const uint32_t blk = it >> 2, q = it & 3u;
+      const ViewDesc& V = views[find_view(views, n_views, blk, KDGR_SCHED_CTA_BLOCKS)];
+      const uint32_t lb = blk - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
+      const int x = (int)(lb % nx) * kBlockW + (int)(q & 1u) * kTileW + (lane & 7);
+      const int y = (int)(lb / nx) * kBlockH + (int)(q >> 1) * kTileH + (lane >> 3);
+      render_px<KB, PACKED, PKT>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
+    }
+  } else if constexpr (SCHED == KDGR_SCHED_SM_STRIPS) {
     // strip of this SM: [total * k / n, total * (k + 1) / n), k = smid mod n
     __shared__ uint32_t s_strip;
     uint32_t smid;
@@ -896,6 +956,7 @@ template <bool PACKED, int KB, bool PKT>
 KernelFn pick_sched_k(const kdgr_batch_config& c) {
   if (c.schedule == KDGR_SCHED_CTA_BLOCKS) return pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS, KB, PKT>(c.min_blocks);
   if (c.schedule == KDGR_SCHED_SM_STRIPS) return pick_minb<PACKED, KDGR_SCHED_SM_STRIPS, KB, PKT>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_WARP_STRIPS) return pick_minb<PACKED, KDGR_SCHED_WARP_STRIPS, KB, PKT>(c.min_blocks);
   return pick_minb<PACKED, KDGR_SCHED_WARP_TILES, KB, PKT>(c.min_blocks);
 }
 
@@ -1009,7 +1070,7 @@ int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
     return KDGR_ERR_INVALID_ARG;
   }
   if (c.schedule != KDGR_SCHED_WARP_TILES && c.schedule != KDGR_SCHED_CTA_BLOCKS &&
-      c.schedule != KDGR_SCHED_SM_STRIPS) {
+      c.schedule != KDGR_SCHED_SM_STRIPS && c.schedule != KDGR_SCHED_WARP_STRIPS) {
     set_error("batch config: unknown schedule");
     return KDGR_ERR_INVALID_ARG;
   }
@@ -1041,10 +1102,12 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
     if (e != cudaSuccess) return e;
     per_sm = occ > 0 ? occ : 1;
   }
-  const bool per_warp = c.schedule == KDGR_SCHED_WARP_TILES;
-  const uint32_t total = per_warp ? total_tiles : total_blocks;
+  const bool warp_strips = c.schedule == KDGR_SCHED_WARP_STRIPS;
+  const bool per_warp = c.schedule == KDGR_SCHED_WARP_TILES || warp_strips;
+  if (warp_strips && total_blocks > 0x3FFFFFFFu) return cudaErrorInvalidValue;
+  const uint32_t total = warp_strips ? 4u * total_blocks : per_warp ? total_tiles : total_blocks;
   // SM strips: the kernel's `chunk` argument carries the number of strips
-  const bool strips = c.schedule == KDGR_SCHED_SM_STRIPS;
+  const bool strips = c.schedule == KDGR_SCHED_SM_STRIPS || warp_strips;
   const int chunk = strips ? std::min(num_sms(), kMaxStrips) : c.chunk;
   uint64_t blocks = (uint64_t)num_sms() * per_sm;
   const uint64_t grabs = strips ? total : ((uint64_t)total + chunk - 1) / chunk;
@@ -1140,53 +1203,55 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
   }
   if (e == cudaSuccess) {
     s->n_aniso = n_aniso;
-    s->d_leaf_packed = A.alloc<uint4>(2 * (size_t)(s->n_offsets ? s->n_offsets : 1));
+    s->d_leaf_packed = A.alloc<uint4>(2 * ((size_t)s->n_pair_entries + 2));
     e = A.err;
   }
-  if (e == cudaSuccess) e = gather_leaf_records(s->d_offsets, s->n_offsets, d_stage, 2, s->d_leaf_packed);
+  if (e == cudaSuccess) e = gather_leaf_records(s->d_pair_gid, s->n_pair_entries, d_stage, 2, s->d_leaf_packed);
   if (d_stage) cudaFree(d_stage);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed upload");
   return KDGR_OK;
 }
 
-__global__ void k_gather_leaf(const uint32_t* __restrict__ offsets, uint32_t n, const uint4* __restrict__ src,
+__global__ void k_gather_leaf(const uint32_t* __restrict__ gid, uint32_t n, const uint4* __restrict__ src,
                               int per, uint4* __restrict__ dst) {
   const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= (size_t)n * per) return;
   const size_t e = j / per, k = j % per;
-  dst[j] = __ldg(src + (size_t)__ldg(offsets + e) * per + k);
+  const uint32_t g = __ldg(gid + e);
+  dst[j] = g == kPadGid ? make_uint4(0u, 0u, 0u, 0u) : __ldg(src + (size_t)g * per + k);
 }
 
-// Pair p of the FP32 leaf records: entries 2p and 2p+1 (the last entry
-// repeated when the count is odd), rows of M and b interleaved lo/hi.
-__global__ void k_build_pairs(const uint32_t* __restrict__ offsets, uint32_t n, const float4* __restrict__ test,
+// Pair p of the FP32 leaf records: entries 2p and 2p+1, rows of M and b
+// interleaved lo/hi; a padding entry gets zeros.
+__global__ void k_build_pairs(const uint32_t* __restrict__ gid, uint32_t n, const float4* __restrict__ test,
                               float4* __restrict__ pairs) {
   const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= ((size_t)n + 1) / 2) return;
-  const uint32_t e0 = (uint32_t)(2 * p), e1 = min(e0 + 1, n - 1);
-  const uint32_t g0 = __ldg(offsets + e0), g1 = __ldg(offsets + e1);
+  if (p >= (size_t)n / 2) return;
+  const uint32_t g0 = __ldg(gid + 2 * p), g1 = __ldg(gid + 2 * p + 1);
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const float4 a = __ldg(test + 3ull * g0 + i), b = __ldg(test + 3ull * g1 + i);
+    const float4 a = g0 == kPadGid ? z : __ldg(test + 3ull * g0 + i);
+    const float4 b = g1 == kPadGid ? z : __ldg(test + 3ull * g1 + i);
     pairs[6 * p + 2 * i] = make_float4(a.x, b.x, a.y, b.y);
     pairs[6 * p + 2 * i + 1] = make_float4(a.z, b.z, a.w, b.w);
   }
 }
 
-cudaError_t build_leaf_pairs(const uint32_t* d_offsets, uint32_t n_offsets, const float4* test, float4* pairs) {
-  if (n_offsets == 0) return cudaSuccess;
-  const size_t np = ((size_t)n_offsets + 1) / 2;
-  k_build_pairs<<<(unsigned)((np + 255) / 256), 256>>>(d_offsets, n_offsets, test, pairs);
+cudaError_t build_leaf_pairs(const uint32_t* d_gid, uint32_t n_entries, const float4* test, float4* pairs) {
+  if (n_entries == 0) return cudaSuccess;
+  const size_t np = (size_t)n_entries / 2;
+  k_build_pairs<<<(unsigned)((np + 255) / 256), 256>>>(d_gid, n_entries, test, pairs);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   return e;
 }
 
-cudaError_t gather_leaf_records(const uint32_t* d_offsets, uint32_t n_offsets, const uint4* src, int per_rec,
+cudaError_t gather_leaf_records(const uint32_t* d_gid, uint32_t n_entries, const uint4* src, int per_rec,
                                 uint4* dst) {
-  if (n_offsets == 0) return cudaSuccess;
-  const size_t total = (size_t)n_offsets * per_rec;
-  k_gather_leaf<<<(unsigned)((total + 255) / 256), 256>>>(d_offsets, n_offsets, src, per_rec, dst);
+  if (n_entries == 0) return cudaSuccess;
+  const size_t total = (size_t)n_entries * per_rec;
+  k_gather_leaf<<<(unsigned)((total + 255) / 256), 256>>>(d_gid, n_entries, src, per_rec, dst);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   return e;

@@ -28,8 +28,13 @@ struct kdgr_scene_s {
   uint4* d_sh_bf16 = nullptr;
   uint32_t* d_aniso_idx = nullptr;
   float4* d_aniso = nullptr;
-  // leaf-major copies of the test records: entry j is the record of
-  // Gaussian offsets[j], so a leaf's candidates are contiguous
+  // leaf-major copies of the test records, padded per leaf to whole pairs:
+  // the fast tree's leaf word y is the leaf's first pair p, its entries are
+  // 2p .. 2p+cnt-1 and an odd leaf ends with one padding entry;
+  // d_pair_gid[j] is the Gaussian of entry j (kPadGid for padding, whose
+  // records are zero)
+  uint32_t* d_pair_gid = nullptr;
+  uint32_t n_pair_entries = 0;     // even
   float4* d_leaf_pairs = nullptr;  // FP32 form, 6 x float4 per pair of entries
   uint4* d_leaf_packed = nullptr;  // packed form, 2 x uint4 per entry
   uint32_t n_aniso = 0;
@@ -72,10 +77,14 @@ void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std:
 // Packed precision form: BF16 SH, FP16 inverse scales / quaternion /
 // opacity, and the FP64 upload-time factors of anisotropic Gaussians.
 int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh, DevAlloc& A);
-// Gather per-Gaussian records (vec16 x per_rec each) into leaf order:
-// dst[j] = src[offsets[j]] for every entry of the ID array.
-cudaError_t build_leaf_pairs(const uint32_t* d_offsets, uint32_t n_offsets, const float4* test, float4* pairs);
-cudaError_t gather_leaf_records(const uint32_t* d_offsets, uint32_t n_offsets, const uint4* src, int per_rec,
+// Fast-form leaf layout: rewrites the leaf words of the relaid tree
+// (y = first pair) and returns the padded per-entry Gaussian IDs.
+void pad_leaf_pairs(std::vector<uint32_t>& relaid, const uint32_t* offsets, std::vector<uint32_t>& pair_gid);
+constexpr uint32_t kPadGid = 0xFFFFFFFFu;
+// Gather per-Gaussian records (vec16 x per_rec each) into padded leaf
+// order: dst[j] = src[gid[j]], zero for padding entries.
+cudaError_t build_leaf_pairs(const uint32_t* d_gid, uint32_t n_entries, const float4* test, float4* pairs);
+cudaError_t gather_leaf_records(const uint32_t* d_gid, uint32_t n_entries, const uint4* src, int per_rec,
                                 uint4* dst);
 // Batched rendering (render_fast.cu).
 // totals: 8x4 tiles, 16x8 blocks and 32x16 super-blocks over all views.

@@ -24,7 +24,7 @@ from . import capi
 from .kdtree import KdTree
 
 FORM_EXACT, FORM_FAST, FORM_PACKED = 0x10, 0x20, 0x40
-SCHED_WARP_TILES, SCHED_CTA_BLOCKS, SCHED_SM_STRIPS = 0, 1, 2
+SCHED_WARP_TILES, SCHED_CTA_BLOCKS, SCHED_SM_STRIPS, SCHED_WARP_STRIPS = 0, 1, 2, 3
 TRAV_PACKET, TRAV_RAY = 0, 1
 SCALES_INVERTED = 0x1
 

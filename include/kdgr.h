@@ -215,6 +215,8 @@ typedef struct {
 #define KDGR_SCHED_SM_STRIPS 2   /* as CTA_BLOCKS, but the blocks are cut into one contiguous strip per
                                     SM; a CTA takes the next block of its SM's strip (neighbours share
                                     the SM's L1) and steals from the following strips when it is done */
+#define KDGR_SCHED_WARP_STRIPS 3 /* as SM_STRIPS, but each warp claims the next 8x4 quarter of a block on its
+                                    own: no CTA barrier between work items */
 
 /* Tree walk of the batch kernel.  Both give every ray its own leaves, in its
  * own front-to-back order, with its own leaf intervals. */

@@ -83,7 +83,7 @@ def test_batch_equals_single_views_and_graph(pkg, cuda, fixtures):
 
 
 def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
-    """Warp tiles, CTA blocks and SM strips (with several chunk sizes and
+    """Warp tiles, CTA blocks, SM strips and warp strips (with several chunk sizes and
     register caps) only change which lane renders which pixel; warp packets
     and per-ray traversal give every ray the same leaves and intervals."""
     fx = fixtures["cluster2k"]
@@ -96,7 +96,8 @@ def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     scene.render_batch(views, len(cams), ref, ref_a)
     for sched, chunk, minb, kb, trav in [(0, 1, 0, 4, 0), (0, 3, 8, 8, 0), (0, 7, 6, 4, 1), (1, 1, 6, 8, 0),
                                          (1, 2, 0, 4, 1), (1, 5, 8, 4, 0), (2, 1, 0, 8, 1), (2, 1, 8, 4, 0),
-                                         (1, 1, 8, 4, 1), (2, 1, 8, 8, 1)]:
+                                         (1, 1, 8, 4, 1), (2, 1, 8, 8, 1), (3, 1, 8, 4, 0), (3, 1, 0, 8, 1),
+                                         (3, 1, 6, 4, 0)]:
         cfg = F.BatchConfig(sched, minb, 0, chunk, 0, kb, trav)
         out = torch.full_like(ref, -1.0)
         out_a = torch.full_like(ref_a, -1.0)
@@ -115,8 +116,8 @@ def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
     views, total, _ = F.make_views(cams)
     rgb = torch.zeros(total * 3, device=cuda)
     best, report = scene.autotune(views, len(cams), rgb)
-    assert best.schedule in (0, 1, 2) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
-    assert len(report.strip().splitlines()) == 17
+    assert best.schedule in (0, 1, 2, 3) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
+    assert len(report.strip().splitlines()) == 20
     assert best.hit_buffer in (4, 8) and best.traversal in (F.TRAV_PACKET, F.TRAV_RAY)
     ref = torch.zeros_like(rgb)
     scene.render_batch(views, len(cams), ref)
@@ -169,7 +170,7 @@ def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
     views, total, _ = F.make_views([(cam, W, H)])
     ref = torch.zeros(total * 3, device=cuda)
     scene.render_batch(views, 1, ref)
-    for sched, kb, trav in [(0, 4, 0), (1, 8, 0), (2, 4, 0), (0, 4, 1), (1, 8, 1)]:
+    for sched, kb, trav in [(0, 4, 0), (1, 8, 0), (2, 4, 0), (3, 4, 0), (0, 4, 1), (1, 8, 1), (3, 8, 1)]:
         out = torch.full_like(ref, -1.0)
         scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, 0, kb, trav))
         torch.cuda.synchronize()
