@@ -52,8 +52,9 @@ struct ExactView {
 //               from the FP64 upload precompute;
 //   leaf_pairs: FP32 form, per pair of leaf entries (2p, 2p+1) the rows of
 //               M = diag(1/s) R^T and b = M mu interleaved lo/hi, 6 x float4;
-//   leaf_packed: packed form, per leaf entry 2 x uint4: (mu.xyz f32, half2
-//               (M22, flag)) and the other eight entries of M as four half2.
+//   leaf_packed: packed form, per pair of leaf entries 4 x uint4: the FP32
+//               means and the FP16 entries of M interleaved lo/hi, and a
+//               flag word (bit k: entry k reads the FP64-precomputed table);
 //   Padding entries hold zero records: M = 0 gives |grdu|^2 = 0 and
 //   t* = 0 * inf = NaN, which no leaf interval accepts.
 struct FastView {

@@ -18,18 +18,18 @@
 //     the record of Gaussian offsets[j]), so a leaf's candidates are one
 //     contiguous run: no ID-then-record dependent load per candidate; the
 //     ID is read only for accepted hits;
-//   * FP32 form: leaf entries are stored in interleaved pairs and tested two
-//     at a time with Blackwell's packed FP32x2 instructions
-//     (fma/mul/sub.rn.f32x2), half the arithmetic instructions per test;
-//   * the precision form reads a leaf's candidates kPipe at a time (all
-//     record loads in flight before the first test);
+//   * both forms store leaf entries in interleaved pairs, padded per leaf,
+//     and test them two at a time with Blackwell's packed FP32x2
+//     instructions (fma/mul/add/sub.rn.f32x2), half the arithmetic
+//     instructions per test;
 //   * warp packets (the default traversal): the 32 rays of an 8x4 tile walk
 //     the tree together, each with its own interval and decisions, so a
 //     leaf's records are warp-uniform loads (pkt_trace below);
 //   * pixels are handed out in spatially coherent units (8x4 warp tiles,
-//     16x8 CTA blocks, or CTA blocks from per-SM contiguous strips) so the
-//     rays sharing an SM's L1 are neighbours; the autotuner picks the
-//     schedule, the register cap (occupancy) and the hit-buffer size.
+//     16x8 CTA blocks, or blocks / tiles from per-SM contiguous strips) so
+//     the rays sharing an SM's L1 are neighbours; the autotuner picks the
+//     schedule, the register cap (occupancy), the hit-buffer size and the
+//     traversal.
 //   * precision form: FP16 rows of M with an FP32 mean and BF16 SH (32 + 96
 //     bytes per Gaussian instead of 48 + 192); Gaussians whose scale ratio
 //     exceeds 1e3 (or whose factors leave the FP16 range) read FP32 factors
@@ -62,14 +62,10 @@ constexpr int kBlockW = 16, kBlockH = 8;  // pixels per CTA block (4 warps of 8x
 #ifndef KDGR_FAST_HITS
 #define KDGR_FAST_HITS 4
 #endif
-#ifndef KDGR_FAST_PIPE
-#define KDGR_FAST_PIPE 2
-#endif
 #ifndef KDGR_FAST_STACK
 #define KDGR_FAST_STACK 12
 #endif
 constexpr int kHits = KDGR_FAST_HITS;  // hit-buffer entries per leaf pass (a leaf averages <1 hit)
-constexpr int kPipe = KDGR_FAST_PIPE;  // candidate records in flight per lane
 
 struct F3 {
   float x, y, z;
@@ -93,66 +89,20 @@ __device__ __forceinline__ float2 h2f(uint32_t w) {
 // (FP64 upload precompute), read as interleaved pairs (load_pair below).
 // Storing Sigma^-1 = M^T M instead would square the condition number (a
 // scale ratio of 2500 gives ~6e6, beyond FP32), so the factor is kept.
-// Packed form (this record): a = (mu, FP16 pair (M22, flag)), b = FP16 pairs
-// of the other eight entries of M; flag != 0 selects the FP64-precomputed
-// table.
-struct Rec {
-  float4 a, b;
-};
-
-// Packed record of leaf entry `pos` (leaf-order copy).
-__device__ __forceinline__ Rec load_rec(const FastView& S, uint32_t pos) {
-  Rec r;
-  const uint4 u0 = __ldg(S.leaf_packed + 2ull * pos), u1 = __ldg(S.leaf_packed + 2ull * pos + 1);
-  r.a = make_float4(__uint_as_float(u0.x), __uint_as_float(u0.y), __uint_as_float(u0.z), __uint_as_float(u0.w));
-  r.b = make_float4(__uint_as_float(u1.x), __uint_as_float(u1.y), __uint_as_float(u1.z), __uint_as_float(u1.w));
-  return r;
-}
-
-// The same test from the rows of M = diag(1/s) R^T (A = M^T M):
-// grdu = M d, t* = -(grdu . gro) / |grdu|^2, gray = |grdu x gro|^2 / |grdu|^2.
-__device__ __forceinline__ bool finish_test(F3 m0, F3 m1, F3 m2, F3 gro, F3 d, float t_near, float t_far,
-                                            float* t_out, float* gray_out) {
-  const F3 grdu = mk(dot3(m0, d), dot3(m1, d), dot3(m2, d));
-  const float r2 = __fdividef(1.f, dot3(grdu, grdu));
-  const float t = -dot3(grdu, gro) * r2;
-  if (!(t >= t_near && t < t_far)) return false;
-  const F3 c = cross3(grdu, gro);
-  const float gray = dot3(c, c) * r2;
-  *t_out = t;
-  *gray_out = gray;
-  return gray < 8.f;
-}
-
-// The test of one packed record (leaf entry `pos`).
-__device__ __forceinline__ bool test_rec(const FastView& S, uint32_t pos, const Rec& r, F3 o, F3 d, float t_near,
-                                         float t_far, float* t_out, float* gray_out) {
-  const float2 m22f = h2f(__float_as_uint(r.a.w));
-  if (m22f.y != 0.f) {  // flagged: factors from the FP64 upload precompute
-    const float4* p = S.aniso + 3ull * __ldg(S.aniso_idx + __ldg(S.offsets + pos));
-    const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
-    const F3 m0 = mk(a.x, a.y, a.z), m1 = mk(b.x, b.y, b.z), m2 = mk(c.x, c.y, c.z);
-    const F3 gro = mk(dot3(m0, o) - a.w, dot3(m1, o) - b.w, dot3(m2, o) - c.w);
-    return finish_test(m0, m1, m2, gro, d, t_near, t_far, t_out, gray_out);
-  }
-  // FP16 rows of M, FP32 mean: gro = M (o - mu) keeps the rounding a small,
-  // consistent perturbation of the Gaussian (no M o - M mu cancellation)
-  const float2 a01 = h2f(__float_as_uint(r.b.x)), a2b0 = h2f(__float_as_uint(r.b.y));
-  const float2 b12 = h2f(__float_as_uint(r.b.z)), c01 = h2f(__float_as_uint(r.b.w));
-  const F3 m0 = mk(a01.x, a01.y, a2b0.x), m1 = mk(a2b0.y, b12.x, b12.y), m2 = mk(c01.x, c01.y, m22f.x);
-  const F3 q = mk(o.x - r.a.x, o.y - r.a.y, o.z - r.a.z);
-  const F3 gro = mk(dot3(m0, q), dot3(m1, q), dot3(m2, q));
-  return finish_test(m0, m1, m2, gro, d, t_near, t_far, t_out, gray_out);
-}
-
 // ------------------------------------------------- paired FP32x2 candidate test
-// The FP32 form stores leaf entries in pairs: pair p holds entries 2p and
-// 2p+1 interleaved, so every quantity of the test is one 64-bit register
-// with entry 2p in the low and entry 2p+1 in the high half, and one packed
-// FP32x2 instruction (fma/mul/sub.rn.f32x2) does the work of two.
-// Pair layout, 6 x 16 bytes, for rows i = 0..2 of M and b:
+// Both forms store leaf entries in pairs: pair p holds entries 2p and 2p+1
+// interleaved, so every quantity of the test is one 64-bit register with
+// entry 2p in the low and entry 2p+1 in the high half, and one packed FP32x2
+// instruction (fma/mul/add/sub.rn.f32x2) does the work of two.
+// FP32 pair, 6 x 16 bytes, for rows i = 0..2 of M and b = M mu:
 //   q[2i]   = (M_i0 lo, M_i0 hi, M_i1 lo, M_i1 hi)
 //   q[2i+1] = (M_i2 lo, M_i2 hi, b_i lo, b_i hi)
+// Packed pair, 4 x 16 bytes (FP32 means, FP16 M as half2 (lo, hi)):
+//   w[0] = (mu.x lo, mu.x hi, mu.y lo, mu.y hi)
+//   w[1] = (mu.z lo, mu.z hi, M00, M01)
+//   w[2] = (M02, M10, M11, M12)
+//   w[3] = (M20, M21, M22, flags)   flags bit k: entry k reads the FP32 factors
+//                                   of the FP64 upload precompute instead
 typedef unsigned long long f2;
 
 __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
@@ -170,6 +120,11 @@ __device__ __forceinline__ f2 sub2(f2 a, f2 b) {
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
   return d;
 }
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+  f2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
 __device__ __forceinline__ f2 bcast2(float x) {
   f2 d;
   asm("mov.b64 %0, {%1, %1};" : "=l"(d) : "f"(x));
@@ -177,6 +132,18 @@ __device__ __forceinline__ f2 bcast2(float x) {
 }
 __device__ __forceinline__ void split2(f2 v, float& lo, float& hi) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 join2(float lo, float hi) {
+  f2 d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+__device__ __forceinline__ f2 h2f2(uint32_t w) {  // half2 -> (lo, hi) FP32 pair
+  const float2 f = h2f(w);
+  return join2(f.x, f.y);
+}
+__device__ __forceinline__ f2 u2f2(uint32_t lo, uint32_t hi) {
+  return join2(__uint_as_float(lo), __uint_as_float(hi));
 }
 
 struct PairRec {
@@ -191,10 +158,6 @@ __device__ __forceinline__ PairRec load_pair(const FastView& S, uint32_t p) {
   return r;
 }
 
-// The M-form test (grdu = M d, gro = M o - b, t* = -(grdu . gro) / |grdu|^2,
-// gray = |grdu x gro|^2 / |grdu|^2) for both entries of a pair.  Works with
-// ng = b - M o = -gro, so t* = (grdu . ng) / |grdu|^2 and the cross product
-// keeps its length.  Returns the pass mask (bit 0: entry 2p, bit 1: 2p+1).
 // Ray constants of the pair test, broadcast to both halves once per leaf.
 struct Ray2 {
   f2 nox, noy, noz, dx, dy, dz;
@@ -203,73 +166,113 @@ __device__ __forceinline__ Ray2 ray2(F3 o, F3 d) {
   return Ray2{bcast2(-o.x), bcast2(-o.y), bcast2(-o.z), bcast2(d.x), bcast2(d.y), bcast2(d.z)};
 }
 
-__device__ __forceinline__ unsigned test_pair(const PairRec& r, const Ray2& w, float t_near, float t_far, float t[2],
-                                              float g[2]) {
-  const f2 nox = w.nox, noy = w.noy, noz = w.noz, dx = w.dx, dy = w.dy, dz = w.dz;
-  f2 ng[3], gd[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const f2 m0 = r.q[2 * i].x, m1 = r.q[2 * i].y, m2 = r.q[2 * i + 1].x, b = r.q[2 * i + 1].y;
-    ng[i] = fma2(m0, nox, fma2(m1, noy, fma2(m2, noz, b)));
-    gd[i] = fma2(m0, dx, fma2(m1, dy, mul2(m2, dz)));
-  }
-  const f2 q = fma2(gd[0], gd[0], fma2(gd[1], gd[1], mul2(gd[2], gd[2])));
-  const f2 a = fma2(gd[0], ng[0], fma2(gd[1], ng[1], mul2(gd[2], ng[2])));
-  float q0, q1, a0, a1;
-  split2(q, q0, q1);
-  split2(a, a0, a1);
-  const float r0 = __fdividef(1.f, q0), r1 = __fdividef(1.f, q1);
-  t[0] = a0 * r0;
-  t[1] = a1 * r1;
-  unsigned m = ((t[0] >= t_near && t[0] < t_far) ? 1u : 0u) | ((t[1] >= t_near && t[1] < t_far) ? 2u : 0u);
-  if (!m) return 0u;
-  const f2 c0 = sub2(mul2(gd[1], ng[2]), mul2(gd[2], ng[1]));
-  const f2 c1 = sub2(mul2(gd[2], ng[0]), mul2(gd[0], ng[2]));
-  const f2 c2 = sub2(mul2(gd[0], ng[1]), mul2(gd[1], ng[0]));
-  const f2 cc = fma2(c0, c0, fma2(c1, c1, mul2(c2, c2)));
-  float cc0, cc1;
-  split2(cc, cc0, cc1);
-  g[0] = cc0 * r0;
-  g[1] = cc1 * r1;
-  if (!(g[0] < 8.f)) m &= ~1u;
-  if (!(g[1] < 8.f)) m &= ~2u;
-  return m;
-}
-
-// test_pair in two steps for warp packets, so the warp can skip the second
-// step (and the hit insertion) together when no lane's t* is in range.
+// The M-form test (grdu = M d, ng = M (mu - o), t* = (grdu . ng) / |grdu|^2,
+// gray = |grdu x ng|^2 / |grdu|^2) for both entries of a pair, in two steps:
+// pair_t decides t* in [t_near, t_far), pair_g the response bound, so a warp
+// packet can skip the second step together when no lane's t* is in range.
 struct PairT {
   f2 ng[3], gd[3];
-  float r0, r1;
+  float q0, q1, a0, a1;
 };
-__device__ __forceinline__ unsigned test_pair_t(const PairRec& r, const Ray2& w, float t_near, float t_far, float t[2],
-                                                PairT& p) {
+__device__ __forceinline__ unsigned pair_t(PairT& p, float t_near, float t_far) {
+  const f2 q = fma2(p.gd[0], p.gd[0], fma2(p.gd[1], p.gd[1], mul2(p.gd[2], p.gd[2])));
+  const f2 a = fma2(p.gd[0], p.ng[0], fma2(p.gd[1], p.ng[1], mul2(p.gd[2], p.ng[2])));
+  // t* = a / q in [t_near, t_far)  <=>  a in [t_near q, t_far q)  (q > 0)
+  const f2 lo = mul2(q, bcast2(t_near)), hi = mul2(q, bcast2(t_far));
+  float q0, q1, a0, a1, l0, l1, h0, h1;
+  split2(q, q0, q1);
+  split2(a, a0, a1);
+  split2(lo, l0, l1);
+  split2(hi, h0, h1);
+  p.q0 = q0;
+  p.q1 = q1;
+  p.a0 = a0;
+  p.a1 = a1;
+  return ((a0 >= l0 && a0 < h0) ? 1u : 0u) | ((a1 >= l1 && a1 < h1) ? 2u : 0u);
+}
+// FP32 pair: ng = b - M o.
+__device__ __forceinline__ void setup_pair(const PairRec& r, const Ray2& w, PairT& p) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     const f2 m0 = r.q[2 * i].x, m1 = r.q[2 * i].y, m2 = r.q[2 * i + 1].x, b = r.q[2 * i + 1].y;
     p.ng[i] = fma2(m0, w.nox, fma2(m1, w.noy, fma2(m2, w.noz, b)));
     p.gd[i] = fma2(m0, w.dx, fma2(m1, w.dy, mul2(m2, w.dz)));
   }
-  const f2 q = fma2(p.gd[0], p.gd[0], fma2(p.gd[1], p.gd[1], mul2(p.gd[2], p.gd[2])));
-  const f2 a = fma2(p.gd[0], p.ng[0], fma2(p.gd[1], p.ng[1], mul2(p.gd[2], p.ng[2])));
-  float q0, q1, a0, a1;
-  split2(q, q0, q1);
-  split2(a, a0, a1);
-  p.r0 = __fdividef(1.f, q0);
-  p.r1 = __fdividef(1.f, q1);
-  t[0] = a0 * p.r0;
-  t[1] = a1 * p.r1;
-  return ((t[0] >= t_near && t[0] < t_far) ? 1u : 0u) | ((t[1] >= t_near && t[1] < t_far) ? 2u : 0u);
 }
-__device__ __forceinline__ unsigned test_pair_g(const PairT& p, unsigned m, float g[2]) {
+
+struct PPairRec {
+  uint4 w[4];
+};
+
+// Packed pair: FP16 rows of M, FP32 mean, ng = M (mu - o) (no M o - M mu
+// cancellation, so the FP16 rounding stays a small consistent perturbation
+// of the Gaussian); flagged entries take the FP64-precomputed factors.
+__device__ __forceinline__ void setup_ppair(const FastView& S, uint32_t pair, const PPairRec& r, const Ray2& w, F3 o,
+                                            F3 d, PairT& p) {
+  const f2 nqx = add2(u2f2(r.w[0].x, r.w[0].y), w.nox);
+  const f2 nqy = add2(u2f2(r.w[0].z, r.w[0].w), w.noy);
+  const f2 nqz = add2(u2f2(r.w[1].x, r.w[1].y), w.noz);
+  const uint32_t mw[9] = {r.w[1].z, r.w[1].w, r.w[2].x, r.w[2].y, r.w[2].z, r.w[2].w, r.w[3].x, r.w[3].y, r.w[3].z};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const f2 m0 = h2f2(mw[3 * i]), m1 = h2f2(mw[3 * i + 1]), m2 = h2f2(mw[3 * i + 2]);
+    p.ng[i] = fma2(m0, nqx, fma2(m1, nqy, mul2(m2, nqz)));
+    p.gd[i] = fma2(m0, w.dx, fma2(m1, w.dy, mul2(m2, w.dz)));
+  }
+  const uint32_t fl = r.w[3].w;
+  if (fl) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (!((fl >> k) & 1u)) continue;
+      const float4* t = S.aniso + 3ull * __ldg(S.aniso_idx + __ldg(S.offsets + 2 * pair + k));
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float4 row = __ldg(t + i);
+        const F3 m = mk(row.x, row.y, row.z);
+        const float ng = row.w - dot3(m, o), gd = dot3(m, d);
+        // replace lane k with integer masks (a split2/join2 round trip with
+        // one half replaced did not store the new half)
+        const unsigned long long sh = k ? 32ull : 0ull;
+        const unsigned long long mask = 0xFFFFFFFFull << sh;
+        p.ng[i] = (p.ng[i] & ~mask) | ((unsigned long long)__float_as_uint(ng) << sh);
+        p.gd[i] = (p.gd[i] & ~mask) | ((unsigned long long)__float_as_uint(gd) << sh);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ PPairRec load_ppair(const FastView& S, uint32_t p) {
+  const uint4* a = S.leaf_packed + 4ull * p;
+  PPairRec r;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r.w[k] = __ldg(a + k);
+  return r;
+}
+
+// The t* step for pair `pair` of either form.
+template <bool PACKED>
+__device__ __forceinline__ unsigned test_pair_t(const FastView& S, uint32_t pair, const Ray2& w, F3 o, F3 d,
+                                                float t_near, float t_far, PairT& p) {
+  if constexpr (PACKED) {
+    setup_ppair(S, pair, load_ppair(S, pair), w, o, d, p);
+  } else {
+    setup_pair(load_pair(S, pair), w, p);
+  }
+  return pair_t(p, t_near, t_far);
+}
+
+__device__ __forceinline__ unsigned test_pair_g(const PairT& p, unsigned m, float t[2], float g[2]) {
+  const float r0 = __fdividef(1.f, p.q0), r1 = __fdividef(1.f, p.q1);
+  t[0] = p.a0 * r0;
+  t[1] = p.a1 * r1;
   const f2 c0 = sub2(mul2(p.gd[1], p.ng[2]), mul2(p.gd[2], p.ng[1]));
   const f2 c1 = sub2(mul2(p.gd[2], p.ng[0]), mul2(p.gd[0], p.ng[2]));
   const f2 c2 = sub2(mul2(p.gd[0], p.ng[1]), mul2(p.gd[1], p.ng[0]));
   const f2 cc = fma2(c0, c0, fma2(c1, c1, mul2(c2, c2)));
   float cc0, cc1;
   split2(cc, cc0, cc1);
-  g[0] = cc0 * p.r0;
-  g[1] = cc1 * p.r1;
+  g[0] = cc0 * r0;
+  g[1] = cc1 * r1;
   if (!(g[0] < 8.f)) m &= ~1u;
   if (!(g[1] < 8.f)) m &= ~2u;
   return m;
@@ -459,32 +462,21 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     HitBuf<K> hb;
     hb.clear();
     bool overflow = false;
-    if constexpr (!PACKED) {
+    {
       const uint32_t np = (cnt + 1) >> 1;
       const Ray2 w = ray2(R.o, R.d);
       for (uint32_t p = 0; p < np; ++p) {
-        const PairRec pr = load_pair(S, pb + p);
         float t2[2], g2[2];
-        const unsigned m = test_pair(pr, w, R.t_near, R.t_far, t2, g2);  // padding: NaN t*, never passes
+        PairT pt;
+        unsigned m = test_pair_t<PACKED>(S, pb + p, w, R.o, R.d, R.t_near, R.t_far, pt);  // padding never passes
+        if (m) {
+          m = test_pair_g(pt, m, t2, g2);
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const uint32_t ik = 2 * p + k;
-          if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
-            overflow |= hb.insert(t2[k], g2[k], ik);
-        }
-      }
-    } else {
-      for (uint32_t i = 0; i < cnt; i += kPipe) {
-        Rec r[kPipe];
-#pragma unroll
-        for (int k = 0; k < kPipe; ++k) r[k] = load_rec(S, base + min(i + k, cnt - 1));
-#pragma unroll
-        for (int k = 0; k < kPipe; ++k) {
-          float t, g;
-          const uint32_t ik = i + k;
-          if (ik < cnt && test_rec(S, base + ik, r[k], R.o, R.d, R.t_near, R.t_far, &t, &g) &&
-              (!have_last || t > last_t || (t == last_t && ik > last_i)))
-            overflow |= hb.insert(t, g, ik);
+          for (int k = 0; k < 2; ++k) {
+            const uint32_t ik = 2 * p + k;
+            if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
+              overflow |= hb.insert(t2[k], g2[k], ik);
+          }
         }
       }
     }
@@ -565,17 +557,16 @@ __device__ __forceinline__ bool pkt_leaf(const FastView& S, uint32_t base, uint3
     hb.clear();
     bool overflow = false;
     const float tn = more ? R.t_near : kInf;
-    if constexpr (!PACKED) {
+    {
       const uint32_t np = (cnt + 1) >> 1;
       const Ray2 w = ray2(R.o, R.d);
       for (uint32_t p = 0; p < np; ++p) {
-        const PairRec pr = load_pair(S, pb + p);
         float t2[2], g2[2];
         PairT pt;
-        unsigned m = test_pair_t(pr, w, tn, R.t_far, t2, pt);  // padding: NaN t*, never passes
+        unsigned m = test_pair_t<PACKED>(S, pb + p, w, R.o, R.d, tn, R.t_far, pt);  // padding never passes
         // warp-uniform branches: most pairs have no lane with t* in range
         if (__any_sync(0xFFFFFFFFu, m != 0u)) {
-          m = test_pair_g(pt, m, g2);
+          m = test_pair_g(pt, m, t2, g2);
           if (__any_sync(0xFFFFFFFFu, m != 0u)) {
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
@@ -584,20 +575,6 @@ __device__ __forceinline__ bool pkt_leaf(const FastView& S, uint32_t base, uint3
                 overflow |= hb.insert(t2[k], g2[k], ik);
             }
           }
-        }
-      }
-    } else {
-      for (uint32_t i = 0; i < cnt; i += kPipe) {
-        Rec r[kPipe];
-#pragma unroll
-        for (int k = 0; k < kPipe; ++k) r[k] = load_rec(S, base + min(i + k, cnt - 1));
-#pragma unroll
-        for (int k = 0; k < kPipe; ++k) {
-          float t, g;
-          const uint32_t ik = i + k;
-          if (ik < cnt && test_rec(S, base + ik, r[k], R.o, R.d, tn, R.t_far, &t, &g) &&
-              (!have_last || t > last_t || (t == last_t && ik > last_i)))
-            overflow |= hb.insert(t, g, ik);
         }
       }
     }
@@ -1206,19 +1183,38 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
     s->d_leaf_packed = A.alloc<uint4>(2 * ((size_t)s->n_pair_entries + 2));
     e = A.err;
   }
-  if (e == cudaSuccess) e = gather_leaf_records(s->d_pair_gid, s->n_pair_entries, d_stage, 2, s->d_leaf_packed);
+  if (e == cudaSuccess)
+    e = build_packed_pairs(s->d_pair_gid, s->n_pair_entries, reinterpret_cast<const uint32_t*>(d_stage),
+                           s->d_leaf_packed);
   if (d_stage) cudaFree(d_stage);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed upload");
   return KDGR_OK;
 }
 
-__global__ void k_gather_leaf(const uint32_t* __restrict__ gid, uint32_t n, const uint4* __restrict__ src,
-                              int per, uint4* __restrict__ dst) {
-  const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= (size_t)n * per) return;
-  const size_t e = j / per, k = j % per;
-  const uint32_t g = __ldg(gid + e);
-  dst[j] = g == kPadGid ? make_uint4(0u, 0u, 0u, 0u) : __ldg(src + (size_t)g * per + k);
+// Pair p of the packed leaf records (layout at PPairRec) from the
+// per-Gaussian staging words: mean x, y, z (FP32), half2 (M22, flag),
+// half2 (M00, M01), (M02, M10), (M11, M12), (M20, M21).  Padding entries
+// are zero.
+__global__ void k_build_ppairs(const uint32_t* __restrict__ gid, uint32_t n, const uint32_t* __restrict__ src,
+                               uint4* __restrict__ out) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (size_t)n / 2) return;
+  uint32_t a[8], b[8];
+  const uint32_t g0 = __ldg(gid + 2 * p), g1 = __ldg(gid + 2 * p + 1);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    a[i] = g0 == kPadGid ? 0u : __ldg(src + 8ull * g0 + i);
+    b[i] = g1 == kPadGid ? 0u : __ldg(src + 8ull * g1 + i);
+  }
+  auto lo = [](uint32_t x) { return x & 0xFFFFu; };
+  auto hi = [](uint32_t x) { return x >> 16; };
+  auto h2 = [](uint32_t l, uint32_t h) { return l | (h << 16); };
+  out[4 * p] = make_uint4(a[0], b[0], a[1], b[1]);
+  out[4 * p + 1] = make_uint4(a[2], b[2], h2(lo(a[4]), lo(b[4])), h2(hi(a[4]), hi(b[4])));
+  out[4 * p + 2] = make_uint4(h2(lo(a[5]), lo(b[5])), h2(hi(a[5]), hi(b[5])), h2(lo(a[6]), lo(b[6])),
+                              h2(hi(a[6]), hi(b[6])));
+  out[4 * p + 3] = make_uint4(h2(lo(a[7]), lo(b[7])), h2(hi(a[7]), hi(b[7])), h2(lo(a[3]), lo(b[3])),
+                              (hi(a[3]) != 0u ? 1u : 0u) | (hi(b[3]) != 0u ? 2u : 0u));
 }
 
 // Pair p of the FP32 leaf records: entries 2p and 2p+1, rows of M and b
@@ -1247,11 +1243,10 @@ cudaError_t build_leaf_pairs(const uint32_t* d_gid, uint32_t n_entries, const fl
   return e;
 }
 
-cudaError_t gather_leaf_records(const uint32_t* d_gid, uint32_t n_entries, const uint4* src, int per_rec,
-                                uint4* dst) {
+cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src, uint4* pairs) {
   if (n_entries == 0) return cudaSuccess;
-  const size_t total = (size_t)n_entries * per_rec;
-  k_gather_leaf<<<(unsigned)((total + 255) / 256), 256>>>(d_gid, n_entries, src, per_rec, dst);
+  const size_t np = (size_t)n_entries / 2;
+  k_build_ppairs<<<(unsigned)((np + 255) / 256), 256>>>(d_gid, n_entries, src, pairs);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   return e;

@@ -36,7 +36,7 @@ struct kdgr_scene_s {
   uint32_t* d_pair_gid = nullptr;
   uint32_t n_pair_entries = 0;     // even
   float4* d_leaf_pairs = nullptr;  // FP32 form, 6 x float4 per pair of entries
-  uint4* d_leaf_packed = nullptr;  // packed form, 2 x uint4 per entry
+  uint4* d_leaf_packed = nullptr;  // packed form, 4 x uint4 per pair of entries
   uint32_t n_aniso = 0;
   // per-scene status word written by kernels (error bits)
   uint32_t* d_status = nullptr;
@@ -81,11 +81,11 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
 // (y = first pair) and returns the padded per-entry Gaussian IDs.
 void pad_leaf_pairs(std::vector<uint32_t>& relaid, const uint32_t* offsets, std::vector<uint32_t>& pair_gid);
 constexpr uint32_t kPadGid = 0xFFFFFFFFu;
-// Gather per-Gaussian records (vec16 x per_rec each) into padded leaf
-// order: dst[j] = src[gid[j]], zero for padding entries.
+// Pair records in padded leaf order (entry j = Gaussian gid[j], zero for
+// padding): FP32 from 3 float4 per Gaussian (rows of M and b), packed from
+// 8 words per Gaussian.
 cudaError_t build_leaf_pairs(const uint32_t* d_gid, uint32_t n_entries, const float4* test, float4* pairs);
-cudaError_t gather_leaf_records(const uint32_t* d_gid, uint32_t n_entries, const uint4* src, int per_rec,
-                                uint4* dst);
+cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src, uint4* pairs);
 // Batched rendering (render_fast.cu).
 // totals: 8x4 tiles, 16x8 blocks and 32x16 super-blocks over all views.
 int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]);
