@@ -102,7 +102,8 @@ __device__ __forceinline__ float2 h2f(uint32_t w) {
 //   w[1] = (mu.z lo, mu.z hi, M00, M01)
 //   w[2] = (M02, M10, M11, M12)
 //   w[3] = (M20, M21, M22, flags)   flags bit k: entry k reads the FP32 factors
-//                                   of the FP64 upload precompute instead
+//                                   of the FP64 upload precompute instead; its
+//                                   mean.x slot then holds the table index
 typedef unsigned long long f2;
 
 __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
@@ -207,8 +208,8 @@ struct PPairRec {
 // Packed pair: FP16 rows of M, FP32 mean, ng = M (mu - o) (no M o - M mu
 // cancellation, so the FP16 rounding stays a small consistent perturbation
 // of the Gaussian); flagged entries take the FP64-precomputed factors.
-__device__ __forceinline__ void setup_ppair(const FastView& S, uint32_t pair, const PPairRec& r, const Ray2& w, F3 o,
-                                            F3 d, PairT& p) {
+__device__ __forceinline__ void setup_ppair(const FastView& S, const PPairRec& r, const Ray2& w, F3 o, F3 d,
+                                            PairT& p) {
   const f2 nqx = add2(u2f2(r.w[0].x, r.w[0].y), w.nox);
   const f2 nqy = add2(u2f2(r.w[0].z, r.w[0].w), w.noy);
   const f2 nqz = add2(u2f2(r.w[1].x, r.w[1].y), w.noz);
@@ -224,7 +225,8 @@ __device__ __forceinline__ void setup_ppair(const FastView& S, uint32_t pair, co
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       if (!((fl >> k) & 1u)) continue;
-      const float4* t = S.aniso + 3ull * __ldg(S.aniso_idx + __ldg(S.offsets + 2 * pair + k));
+      // a flagged entry's mean.x slot holds its index into the FP64 table
+      const float4* t = S.aniso + 3ull * (k ? r.w[0].y : r.w[0].x);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         const float4 row = __ldg(t + i);
@@ -254,7 +256,7 @@ template <bool PACKED>
 __device__ __forceinline__ unsigned test_pair_t(const FastView& S, uint32_t pair, const Ray2& w, F3 o, F3 d,
                                                 float t_near, float t_far, PairT& p) {
   if constexpr (PACKED) {
-    setup_ppair(S, pair, load_ppair(S, pair), w, o, d, p);
+    setup_ppair(S, load_ppair(S, pair), w, o, d, p);
   } else {
     setup_pair(load_pair(S, pair), w, p);
   }
@@ -1185,7 +1187,7 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
   }
   if (e == cudaSuccess)
     e = build_packed_pairs(s->d_pair_gid, s->n_pair_entries, reinterpret_cast<const uint32_t*>(d_stage),
-                           s->d_leaf_packed);
+                           s->d_aniso_idx, s->d_leaf_packed);
   if (d_stage) cudaFree(d_stage);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed upload");
   return KDGR_OK;
@@ -1194,9 +1196,9 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
 // Pair p of the packed leaf records (layout at PPairRec) from the
 // per-Gaussian staging words: mean x, y, z (FP32), half2 (M22, flag),
 // half2 (M00, M01), (M02, M10), (M11, M12), (M20, M21).  Padding entries
-// are zero.
+// are zero; a flagged entry's mean.x becomes its FP64-table index.
 __global__ void k_build_ppairs(const uint32_t* __restrict__ gid, uint32_t n, const uint32_t* __restrict__ src,
-                               uint4* __restrict__ out) {
+                               const uint32_t* __restrict__ aniso_idx, uint4* __restrict__ out) {
   const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= (size_t)n / 2) return;
   uint32_t a[8], b[8];
@@ -1209,6 +1211,9 @@ __global__ void k_build_ppairs(const uint32_t* __restrict__ gid, uint32_t n, con
   auto lo = [](uint32_t x) { return x & 0xFFFFu; };
   auto hi = [](uint32_t x) { return x >> 16; };
   auto h2 = [](uint32_t l, uint32_t h) { return l | (h << 16); };
+  // flagged entries carry their FP64-table index in place of mean.x
+  if (hi(a[3]) != 0u) a[0] = __ldg(aniso_idx + g0);
+  if (hi(b[3]) != 0u) b[0] = __ldg(aniso_idx + g1);
   out[4 * p] = make_uint4(a[0], b[0], a[1], b[1]);
   out[4 * p + 1] = make_uint4(a[2], b[2], h2(lo(a[4]), lo(b[4])), h2(hi(a[4]), hi(b[4])));
   out[4 * p + 2] = make_uint4(h2(lo(a[5]), lo(b[5])), h2(hi(a[5]), hi(b[5])), h2(lo(a[6]), lo(b[6])),
@@ -1243,10 +1248,11 @@ cudaError_t build_leaf_pairs(const uint32_t* d_gid, uint32_t n_entries, const fl
   return e;
 }
 
-cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src, uint4* pairs) {
+cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src,
+                               const uint32_t* aniso_idx, uint4* pairs) {
   if (n_entries == 0) return cudaSuccess;
   const size_t np = (size_t)n_entries / 2;
-  k_build_ppairs<<<(unsigned)((np + 255) / 256), 256>>>(d_gid, n_entries, src, pairs);
+  k_build_ppairs<<<(unsigned)((np + 255) / 256), 256>>>(d_gid, n_entries, src, aniso_idx, pairs);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   return e;

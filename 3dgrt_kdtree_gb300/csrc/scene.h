@@ -85,7 +85,8 @@ constexpr uint32_t kPadGid = 0xFFFFFFFFu;
 // padding): FP32 from 3 float4 per Gaussian (rows of M and b), packed from
 // 8 words per Gaussian.
 cudaError_t build_leaf_pairs(const uint32_t* d_gid, uint32_t n_entries, const float4* test, float4* pairs);
-cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src, uint4* pairs);
+cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src,
+                               const uint32_t* aniso_idx, uint4* pairs);
 // Batched rendering (render_fast.cu).
 // totals: 8x4 tiles, 16x8 blocks and 32x16 super-blocks over all views.
 int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]);
