@@ -73,6 +73,7 @@ void kdgr_batch_config_default(kdgr_batch_config* c) {
   c->precision = 0;
   c->hit_buffer = 4;
   c->traversal = KDGR_TRAV_PACKET;
+  c->tile_shape = KDGR_TILE_8X4;
 }
 
 int kdgr_render_batch(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb, float* alpha, float* depth,
@@ -221,9 +222,10 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
   cudaEventCreate(&e1);
   std::string rep;
   float best_ms = 1e30f;
-  // stage 1: schedule x register cap x chunk with warp packets and the
-  // 4-entry hit buffer; stage 2: the winner with the 8-entry buffer (dense
-  // leaves re-scan less) and the winner with per-ray traversal
+  // stage 1: schedule x register cap x chunk with warp packets, 8x4 tiles
+  // and the 4-entry hit buffer; stage 2: the winner with the 8-entry buffer
+  // (dense leaves re-scan less), with per-ray traversal, and with 4x8 and
+  // 16x2 warp tiles
   bool stage2 = false;
   for (size_t ci = 0; ci < cands.size() || !stage2; ++ci) {
     if (ci == cands.size()) {  // reached once: appends the stage-2 candidates
@@ -234,6 +236,12 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
       cr.traversal = KDGR_TRAV_RAY;
       cands.push_back(c8);
       cands.push_back(cr);
+      if (best->schedule != KDGR_SCHED_WARP_TILES)
+        for (int tile : {KDGR_TILE_4X8, KDGR_TILE_16X2}) {
+          kdgr_batch_config ct = *best;
+          ct.tile_shape = tile;
+          cands.push_back(ct);
+        }
     }
     const kdgr_batch_config c = cands[ci];
     rc = run_once(s, c, table, totals, rgb, nullptr, nullptr, st, "kdgr_autotune");  // warm-up
@@ -254,8 +262,8 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
     char line[256];
     snprintf(line, sizeof(line),
              "{\"schedule\": %d, \"min_blocks\": %d, \"chunk\": %d, \"precision\": %d, \"hit_buffer\": %d, "
-             "\"traversal\": %d, \"ms\": %.4f}\n",
-             c.schedule, c.min_blocks, c.chunk, c.precision, c.hit_buffer, c.traversal, med);
+             "\"traversal\": %d, \"tile_shape\": %d, \"ms\": %.4f}\n",
+             c.schedule, c.min_blocks, c.chunk, c.precision, c.hit_buffer, c.traversal, c.tile_shape, med);
     rep += line;
     if (med < best_ms) {
       best_ms = med;

@@ -759,6 +759,22 @@ __device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, 
   }
 }
 
+// Pixel of lane `lane` in quarter q (0..3) of the 16x8 block whose top-left
+// pixel is (bx, by), for the warp tile shape (KDGR_TILE_*): 8x4 tiles in a
+// 2x2 arrangement, 4x8 tiles side by side, or 16x2 tiles stacked.
+__device__ __forceinline__ void block_pixel(int tile, int bx, int by, int q, int lane, int& x, int& y) {
+  if (tile == KDGR_TILE_4X8) {
+    x = bx + 4 * q + (lane & 3);
+    y = by + (lane >> 2);
+  } else if (tile == KDGR_TILE_16X2) {
+    x = bx + (lane & 15);
+    y = by + 2 * q + (lane >> 4);
+  } else {
+    x = bx + (q & 1) * kTileW + (lane & 7);
+    y = by + (q >> 1) * kTileH + (lane >> 3);
+  }
+}
+
 // Persistent kernel.  Schedules (include/kdgr.h):
 //   WARP_TILES: each warp takes `chunk` 8x4 tiles from the global queue;
 //   WARP_STRIPS: each warp takes the next 8x4 tile (in 16x8-block order) of
@@ -774,7 +790,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
                                                                  float* __restrict__ rgb,
                                                                  float* __restrict__ alpha_out,
                                                                  float* __restrict__ depth_out, uint32_t* queue,
-                                                                 uint32_t* status, int chunk) {
+                                                                 uint32_t* status, int chunk, int tile) {
   __shared__ uint32_t s_id[kStack][kThreads];
   __shared__ float s_t[kStack][kThreads];
   __shared__ PktEnt s_ent[kStack][kWarps];
@@ -800,8 +816,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
       const uint32_t blk = it >> 2, q = it & 3u;
       const ViewDesc& V = views[find_view(views, n_views, blk, KDGR_SCHED_CTA_BLOCKS)];
       const uint32_t lb = blk - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
-      const int x = (int)(lb % nx) * kBlockW + (int)(q & 1u) * kTileW + (lane & 7);
-      const int y = (int)(lb / nx) * kBlockH + (int)(q >> 1) * kTileH + (lane >> 3);
+      int x, y;
+      block_pixel(tile, (int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, (int)q, lane, x, y);
       render_px<KB, PACKED, PKT>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
     }
   } else if constexpr (SCHED == KDGR_SCHED_SM_STRIPS) {
@@ -829,8 +845,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
       }
       const ViewDesc& V = views[find_view(views, n_views, item, KDGR_SCHED_CTA_BLOCKS)];
       const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
-      const int x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
-      const int y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
+      int x, y;
+      block_pixel(tile, (int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, warp, lane, x, y);
       render_px<KB, PACKED, PKT>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
     }
   } else {
@@ -853,8 +869,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
         int x, y;
         if (SCHED == KDGR_SCHED_CTA_BLOCKS) {
           const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
-          x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
-          y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
+          block_pixel(tile, (int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, warp, lane, x, y);
         } else {
           const uint32_t lt = item - __ldg(&V.wt_base), nx = __ldg(&V.wt_x);
           x = (int)(lt % nx) * kTileW + (lane & 7);
@@ -922,7 +937,7 @@ __global__ void k_aniso_fp64(const float* __restrict__ src, uint32_t n, float4* 
 }
 
 using KernelFn = void (*)(FastView, const ViewDesc*, int, uint32_t, float*, float*, float*, uint32_t*, uint32_t*,
-                          int);
+                          int, int);
 
 template <bool PACKED, int SCHED, int KB, bool PKT>
 KernelFn pick_minb(int minb) {
@@ -1061,6 +1076,14 @@ int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
     set_error("batch config: min_blocks must be 0, 6 or 8");
     return KDGR_ERR_INVALID_ARG;
   }
+  if (c.tile_shape != KDGR_TILE_8X4 && c.tile_shape != KDGR_TILE_4X8 && c.tile_shape != KDGR_TILE_16X2) {
+    set_error("batch config: tile_shape must be KDGR_TILE_8X4, KDGR_TILE_4X8 or KDGR_TILE_16X2");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (c.tile_shape != KDGR_TILE_8X4 && c.schedule == KDGR_SCHED_WARP_TILES) {
+    set_error("batch config: the warp-tile schedule renders 8x4 tiles only");
+    return KDGR_ERR_INVALID_ARG;
+  }
   if (c.traversal != KDGR_TRAV_PACKET && c.traversal != KDGR_TRAV_RAY) {
     set_error("batch config: traversal must be KDGR_TRAV_PACKET or KDGR_TRAV_RAY");
     return KDGR_ERR_INVALID_ARG;
@@ -1093,7 +1116,8 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
   const uint64_t cap = per_warp ? (grabs + kWarps - 1) / kWarps : grabs;
   if (blocks > cap) blocks = cap > 0 ? cap : 1;
   fn<<<(unsigned)blocks, kThreads, 0, st>>>(s->fast_view(), d_views, n_views, total, rgb, alpha, depth, queue,
-                                            s->d_status, chunk);
+                                            s->d_status, chunk,
+                                            c.tile_shape);
   return cudaGetLastError();
 }
 

@@ -26,6 +26,7 @@ from .kdtree import KdTree
 FORM_EXACT, FORM_FAST, FORM_PACKED = 0x10, 0x20, 0x40
 SCHED_WARP_TILES, SCHED_CTA_BLOCKS, SCHED_SM_STRIPS, SCHED_WARP_STRIPS = 0, 1, 2, 3
 TRAV_PACKET, TRAV_RAY = 0, 1
+TILE_8X4, TILE_4X8, TILE_16X2 = 0, 1, 2
 SCALES_INVERTED = 0x1
 
 
@@ -44,7 +45,7 @@ class View(ctypes.Structure):
 class BatchConfig(ctypes.Structure):
     _fields_ = [("schedule", ctypes.c_int32), ("min_blocks", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("chunk", ctypes.c_int32), ("precision", ctypes.c_int32), ("hit_buffer", ctypes.c_int32),
-                ("traversal", ctypes.c_int32)]
+                ("traversal", ctypes.c_int32), ("tile_shape", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -224,6 +224,12 @@ typedef struct {
                               when any ray needs it); leaf records become warp-uniform loads */
 #define KDGR_TRAV_RAY 1    /* each lane walks its own ray independently */
 
+/* Pixel tile of one warp (32 rays) inside a 16x8 block; the warp-tile
+ * schedule renders 8x4 tiles only. */
+#define KDGR_TILE_8X4 0
+#define KDGR_TILE_4X8 1
+#define KDGR_TILE_16X2 2
+
 typedef struct {
   int32_t schedule;      /* KDGR_SCHED_* */
   int32_t min_blocks;    /* register cap: 0 (compiler), 6 or 8 resident 128-thread CTAs per SM */
@@ -233,6 +239,7 @@ typedef struct {
   int32_t hit_buffer;    /* per-leaf register hit buffer: 4 or 8 entries (0 = 4); a leaf with more
                             accepted hits is re-scanned for the next ones */
   int32_t traversal;     /* KDGR_TRAV_*: how the rays of a warp walk the tree */
+  int32_t tile_shape;    /* KDGR_TILE_*: the warp's pixel tile inside each 16x8 block */
 } kdgr_batch_config;
 
 void kdgr_batch_config_default(kdgr_batch_config* cfg);

@@ -85,7 +85,8 @@ def test_batch_equals_single_views_and_graph(pkg, cuda, fixtures):
 def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     """Warp tiles, CTA blocks, SM strips and warp strips (with several chunk sizes and
     register caps) only change which lane renders which pixel; warp packets
-    and per-ray traversal give every ray the same leaves and intervals."""
+    and per-ray traversal give every ray the same leaves and intervals, for
+    every warp tile shape."""
     fx = fixtures["cluster2k"]
     F = pkg.renderer
     scene = F.Scene(fx.tree, fx.rec)
@@ -94,17 +95,18 @@ def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     ref = torch.zeros(total * 3, device=cuda)
     ref_a = torch.zeros(total, device=cuda)
     scene.render_batch(views, len(cams), ref, ref_a)
-    for sched, chunk, minb, kb, trav in [(0, 1, 0, 4, 0), (0, 3, 8, 8, 0), (0, 7, 6, 4, 1), (1, 1, 6, 8, 0),
-                                         (1, 2, 0, 4, 1), (1, 5, 8, 4, 0), (2, 1, 0, 8, 1), (2, 1, 8, 4, 0),
-                                         (1, 1, 8, 4, 1), (2, 1, 8, 8, 1), (3, 1, 8, 4, 0), (3, 1, 0, 8, 1),
-                                         (3, 1, 6, 4, 0)]:
-        cfg = F.BatchConfig(sched, minb, 0, chunk, 0, kb, trav)
+    for sched, chunk, minb, kb, trav, tile in [(0, 1, 0, 4, 0, 0), (0, 3, 8, 8, 0, 0), (0, 7, 6, 4, 1, 0),
+                                               (1, 1, 6, 8, 0, 1), (1, 2, 0, 4, 1, 2), (1, 5, 8, 4, 0, 0),
+                                               (2, 1, 0, 8, 1, 0), (2, 1, 8, 4, 0, 2), (1, 1, 8, 4, 1, 1),
+                                               (2, 1, 8, 8, 1, 1), (3, 1, 8, 4, 0, 0), (3, 1, 0, 8, 1, 2),
+                                               (3, 1, 6, 4, 0, 1)]:
+        cfg = F.BatchConfig(sched, minb, 0, chunk, 0, kb, trav, tile)
         out = torch.full_like(ref, -1.0)
         out_a = torch.full_like(ref_a, -1.0)
         scene.render_batch(views, len(cams), out, out_a, cfg=cfg)
         torch.cuda.synchronize()
-        assert float((out - ref).abs().max()) <= 1e-5, (sched, chunk, minb, trav)
-        assert float((out_a - ref_a).abs().max()) <= 1e-5, (sched, chunk, minb, trav)
+        assert float((out - ref).abs().max()) <= 1e-5, (sched, chunk, minb, trav, tile)
+        assert float((out_a - ref_a).abs().max()) <= 1e-5, (sched, chunk, minb, trav, tile)
     scene.close()
 
 
@@ -117,8 +119,11 @@ def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
     rgb = torch.zeros(total * 3, device=cuda)
     best, report = scene.autotune(views, len(cams), rgb)
     assert best.schedule in (0, 1, 2, 3) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
-    assert len(report.strip().splitlines()) == 20
+    # 18 stage-1 lines, then 8-entry buffer, per-ray traversal and (unless the
+    # warp-tile schedule won stage 1) the 4x8 and 16x2 tile shapes
+    assert len(report.strip().splitlines()) in (20, 22)
     assert best.hit_buffer in (4, 8) and best.traversal in (F.TRAV_PACKET, F.TRAV_RAY)
+    assert best.tile_shape in (F.TILE_8X4, F.TILE_4X8, F.TILE_16X2)
     ref = torch.zeros_like(rgb)
     scene.render_batch(views, len(cams), ref)
     out = torch.zeros_like(rgb)
@@ -136,6 +141,12 @@ def test_batch_config_errors(pkg, cuda, fixtures):
     rgb = torch.zeros(total * 3, device=cuda)
     with pytest.raises(pkg.capi.KdgrError):
         scene.render_batch(views, 1, rgb)  # no fast arrays materialised
+    scene.close()
+    scene = F.Scene(fx.tree, fx.rec)
+    for bad in (F.BatchConfig(0, 8, 0, 1, 0, 4, 0, F.TILE_4X8),  # warp tiles are 8x4 only
+                F.BatchConfig(1, 8, 0, 1, 0, 4, 0, 7), F.BatchConfig(1, 8, 0, 1, 0, 4, 5, 0)):
+        with pytest.raises(pkg.capi.KdgrError):
+            scene.render_batch(views, 1, rgb, cfg=bad)
     scene.close()
 
 
@@ -170,9 +181,10 @@ def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
     views, total, _ = F.make_views([(cam, W, H)])
     ref = torch.zeros(total * 3, device=cuda)
     scene.render_batch(views, 1, ref)
-    for sched, kb, trav in [(0, 4, 0), (1, 8, 0), (2, 4, 0), (3, 4, 0), (0, 4, 1), (1, 8, 1), (3, 8, 1)]:
+    for sched, kb, trav, tile in [(0, 4, 0, 0), (1, 8, 0, 1), (2, 4, 0, 2), (3, 4, 0, 1), (0, 4, 1, 0),
+                                  (1, 8, 1, 2), (3, 8, 1, 0)]:
         out = torch.full_like(ref, -1.0)
-        scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, 0, kb, trav))
+        scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, 0, kb, trav, tile))
         torch.cuda.synchronize()
         np.testing.assert_array_equal(out.cpu().numpy(), ref.cpu().numpy())
     assert scene.status() == 0
