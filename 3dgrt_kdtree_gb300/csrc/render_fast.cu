@@ -5,31 +5,32 @@
 // traversal front to back, per-leaf max-response test, hits composited in t
 // order until the opacity threshold.  What changes, for throughput:
 //   * arithmetic: FMA, fast reciprocal, __expf; the ray-Gaussian test reads
-//     the precomputed rows of M = diag(1/s) R^T with b = M mu folded in
-//     (gro = M o - b, grdu = M d) and rejects on t* before evaluating the
+//     the precomputed rows of M = diag(1/s) R^T (with b = M mu folded in for
+//     the FP32 form), forms ng = M (mu - o) and grdu = M d, accepts t* on
+//     the leaf interval without a reciprocal and only then evaluates the
 //     Mahalanobis distance;
 //   * hits are accepted with t* in the half-open interval [t_near, t_far),
 //     so a Gaussian straddling a split plane is composited in one leaf only;
 //   * the tree is relaid out with its top levels breadth-first (they stay
-//     hot in L1/L2) and the rest depth-first;
+//     hot in L1/L2) and the rest depth-first, and validated at upload, so
+//     node steps carry no bounds checks;
 //   * the short stack (ring semantics and root restart as the reference) is
 //     in shared memory, [slot][thread];
-//   * candidate records are stored a second time in leaf order (entry j is
-//     the record of Gaussian offsets[j]), so a leaf's candidates are one
-//     contiguous run: no ID-then-record dependent load per candidate; the
-//     ID is read only for accepted hits;
-//   * both forms store leaf entries in interleaved pairs, padded per leaf,
-//     and test them two at a time with Blackwell's packed FP32x2
-//     instructions (fma/mul/add/sub.rn.f32x2), half the arithmetic
-//     instructions per test;
-//   * warp packets (the default traversal): the 32 rays of an 8x4 tile walk
+//   * candidate records are stored a second time in leaf order, padded to
+//     whole pairs per leaf, so a leaf's candidates are one contiguous run:
+//     no ID-then-record dependent load per candidate; the ID is read only
+//     for accepted hits;
+//   * both forms store leaf entries in interleaved pairs and test them two
+//     at a time with Blackwell's packed FP32x2 instructions
+//     (fma/mul/add/sub.rn.f32x2), half the arithmetic instructions per test;
+//   * warp packets (the default traversal): the 32 rays of a warp tile walk
 //     the tree together, each with its own interval and decisions, so a
 //     leaf's records are warp-uniform loads (pkt_trace below);
 //   * pixels are handed out in spatially coherent units (8x4 warp tiles,
 //     16x8 CTA blocks, or blocks / tiles from per-SM contiguous strips) so
 //     the rays sharing an SM's L1 are neighbours; the autotuner picks the
-//     schedule, the register cap (occupancy), the hit-buffer size and the
-//     traversal.
+//     schedule, the register cap (occupancy), the hit-buffer size, the
+//     traversal and the warp tile shape;
 //   * precision form: FP16 rows of M with an FP32 mean and BF16 SH (32 + 96
 //     bytes per Gaussian instead of 48 + 192); Gaussians whose scale ratio
 //     exceeds 1e3 (or whose factors leave the FP16 range) read FP32 factors
@@ -58,7 +59,7 @@ namespace {
 constexpr int kWarps = 4;
 constexpr int kThreads = kWarps * 32;
 constexpr int kTileW = 8, kTileH = 4;     // pixels per warp tile
-constexpr int kBlockW = 16, kBlockH = 8;  // pixels per CTA block (4 warps of 8x4)
+constexpr int kBlockW = 16, kBlockH = 8;  // pixels per CTA block (4 warp tiles)
 #ifndef KDGR_FAST_HITS
 #define KDGR_FAST_HITS 4
 #endif
@@ -526,7 +527,7 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
 }
 
 // ------------------------------------------------------------ warp packets
-// Packet traversal of one 8x4 warp tile: the warp walks the tree together.
+// Packet traversal of one warp tile (32 rays): the warp walks the tree together.
 // Primary rays of a tile share the eye point and, away from the image lines
 // where a direction component changes sign, the sign of every direction
 // component, so the front-to-back child order at a node is the same for all
@@ -777,7 +778,7 @@ __device__ __forceinline__ void block_pixel(int tile, int bx, int by, int q, int
 
 // Persistent kernel.  Schedules (include/kdgr.h):
 //   WARP_TILES: each warp takes `chunk` 8x4 tiles from the global queue;
-//   WARP_STRIPS: each warp takes the next 8x4 tile (in 16x8-block order) of
+//   WARP_STRIPS: each warp takes the next quarter of a 16x8 block of
 //               its SM's strip of the block list, then steals from the
 //               following strips;
 //   CTA_BLOCKS: each CTA takes `chunk` 16x8 blocks (barrier per block) and
@@ -797,7 +798,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
   __shared__ uint32_t s_work;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if constexpr (SCHED == KDGR_SCHED_WARP_STRIPS) {
-    // items are quarters of 16x8 blocks (8x4 tiles in block order); each
+    // items are quarters of 16x8 blocks (warp tiles in block order); each
     // warp claims the next quarter of its SM's strip, no CTA barrier
     uint32_t smid;
     asm("mov.u32 %0, %%smid;" : "=r"(smid));

@@ -197,7 +197,7 @@ int kdgr_render(kdgr_scene_t scene, const kdgr_camera* cam, int width, int heigh
 
 /* ------------------------------------------------------- batched rendering
  * The batching, precision and serving forms.  One persistent launch draws
- * 8x4-pixel ray tiles of every queued view from an atomic work queue.  These
+ * 32-ray pixel tiles of every queued view from an atomic work queue.  These
  * forms use fast FP32 arithmetic (FMA, rsqrt, exp2 approximation) and accept
  * hits with t* in the half-open leaf interval [t_near, t_far); they agree
  * with the FP64 oracle to <= 1e-3 RMSE.  No reference counterpart: the
@@ -215,12 +215,12 @@ typedef struct {
 #define KDGR_SCHED_SM_STRIPS 2   /* as CTA_BLOCKS, but the blocks are cut into one contiguous strip per
                                     SM; a CTA takes the next block of its SM's strip (neighbours share
                                     the SM's L1) and steals from the following strips when it is done */
-#define KDGR_SCHED_WARP_STRIPS 3 /* as SM_STRIPS, but each warp claims the next 8x4 quarter of a block on its
+#define KDGR_SCHED_WARP_STRIPS 3 /* as SM_STRIPS, but each warp claims the next quarter of a block on its
                                     own: no CTA barrier between work items */
 
 /* Tree walk of the batch kernel.  Both give every ray its own leaves, in its
  * own front-to-back order, with its own leaf intervals. */
-#define KDGR_TRAV_PACKET 0 /* the 32 rays of a warp's 8x4 tile walk the tree together (a child is entered
+#define KDGR_TRAV_PACKET 0 /* the 32 rays of a warp's tile walk the tree together (a child is entered
                               when any ray needs it); leaf records become warp-uniform loads */
 #define KDGR_TRAV_RAY 1    /* each lane walks its own ray independently */
 
