@@ -161,7 +161,7 @@ typedef struct {
   uint32_t n_nodes, n_offsets, n_gaussians;
   uint32_t depth, n_leaves, max_leaf;
   uint32_t forms;         /* KDGR_FORM_* present */
-  uint32_t top_nodes;     /* fast form: nodes staged in shared memory */
+  uint32_t top_nodes;     /* fast form: nodes of the breadth-first top (10 levels) of the relaid tree */
   uint32_t n_aniso;       /* packed form: Gaussians with FP64-precomputed factors */
   uint64_t device_bytes;  /* HBM held by the scene */
 } kdgr_scene_info;
