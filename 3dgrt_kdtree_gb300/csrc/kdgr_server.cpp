@@ -225,7 +225,7 @@ void kdgr_server_s::scheduler() {
     const bool packed = cfg.precision != 0;
     lk.unlock();
     cudaError_t e = cudaMemcpyAsync(L.d_views, L.h_views, k * sizeof(ViewDesc), cudaMemcpyHostToDevice, L.st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(L.d_queue, 0, 4, L.st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(L.d_queue, 0, kQueueBytes, L.st);
     if (e == cudaSuccess)
       e = launch_multi(d_scenes, packed, L.d_views, (int)k, (uint32_t)cbase, d_arena, L.d_queue, d_status, L.st);
     if (e == cudaSuccess) e = cudaEventRecord(L.ev, L.st);
@@ -327,7 +327,7 @@ int kdgr_server_create(const kdgr_server_config* cfg, kdgr_server_t* out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&L.d_views, sizeof(ViewDesc) * c.max_views_per_launch);
     if (e == cudaSuccess) e = cudaMallocHost(&L.h_views, sizeof(ViewDesc) * c.max_views_per_launch);
-    if (e == cudaSuccess) e = cudaMalloc(&L.d_queue, 4);
+    if (e == cudaSuccess) e = cudaMalloc(&L.d_queue, kQueueBytes);
   }
   if (e != cudaSuccess) {
     kdgr_server_destroy(s.release());

@@ -882,31 +882,40 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
   }
 }
 
-// Multi-scene form of the CTA-block schedule for the serving loop: every view
-// names a scene slot and the CTA renders each block against that slot's
-// arrays (scenes[] in device memory).  One persistent launch serves the
-// requests of all resident scenes queued in a tick.
+// Multi-scene form of the warp-strip schedule for the serving loop: every
+// view names a scene slot and each warp renders its quarter-block against
+// that slot's arrays (scenes[] in device memory).  One persistent launch
+// serves the requests of all resident scenes queued in a tick.  Items are
+// quarters of 16x8 blocks; queue word 1 + k counts the claims of strip k.
 template <bool PACKED>
 __global__ void __launch_bounds__(kThreads, 8) k_render_multi(const FastView* __restrict__ scenes,
                                                               const ViewDesc* __restrict__ views, int n_views,
                                                               uint32_t total_items, float* __restrict__ rgb,
-                                                              uint32_t* queue, uint32_t* status) {
+                                                              uint32_t* queue, uint32_t* status, int n_strips) {
   __shared__ uint32_t s_id[kStack][kThreads];
   __shared__ float s_t[kStack][kThreads];
   __shared__ PktEnt s_ent[kStack][kWarps];
-  __shared__ uint32_t s_work;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  while (true) {
-    __syncthreads();
-    if (tid == 0) s_work = atomicAdd(queue, 1u);
-    __syncthreads();
-    const uint32_t item = s_work;
-    if (item >= total_items) break;
-    const ViewDesc& V = views[find_view(views, n_views, item, KDGR_SCHED_CTA_BLOCKS)];
+  const int tid = threadIdx.x, lane = tid & 31;
+  uint32_t smid;
+  asm("mov.u32 %0, %%smid;" : "=r"(smid));
+  const uint32_t n = (uint32_t)n_strips;
+  uint32_t k = smid % n, visited = 0;
+  while (visited < n) {
+    const uint32_t b0 = (uint32_t)((uint64_t)total_items * k / n), b1 = (uint32_t)((uint64_t)total_items * (k + 1) / n);
+    uint32_t it = 0;
+    if (lane == 0) it = b0 + atomicAdd(queue + 1 + k, 1u);
+    it = __shfl_sync(0xFFFFFFFFu, it, 0);
+    if (it >= b1) {
+      k = (k + 1) % n;
+      ++visited;
+      continue;
+    }
+    const uint32_t blk = it >> 2;
+    const ViewDesc& V = views[find_view(views, n_views, blk, KDGR_SCHED_CTA_BLOCKS)];
     const FastView& S = scenes[__ldg(&V.scene)];
-    const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
-    const int x = (int)(lb % nx) * kBlockW + (warp & 1) * kTileW + (lane & 7);
-    const int y = (int)(lb / nx) * kBlockH + (warp >> 1) * kTileH + (lane >> 3);
+    const uint32_t lb = blk - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
+    int x, y;
+    block_pixel(KDGR_TILE_8X4, (int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, (int)(it & 3u), lane, x, y);
     render_px<kHits, PACKED, true>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, nullptr, nullptr, status);
   }
 }
@@ -1291,9 +1300,13 @@ cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* 
   int occ = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreads, 0);
   if (e != cudaSuccess) return e;
+  if (total_blocks > 0x3FFFFFFFu) return cudaErrorInvalidValue;
+  const uint32_t quarters = 4u * total_blocks;
   uint64_t blocks = (uint64_t)num_sms() * (occ > 0 ? occ : 1);
-  if (blocks > total_blocks) blocks = total_blocks > 0 ? total_blocks : 1;
-  fn<<<(unsigned)blocks, kThreads, 0, st>>>(d_scenes, d_views, n_views, total_blocks, rgb, queue, status);
+  const uint64_t cap = ((uint64_t)quarters + kWarps - 1) / kWarps;
+  if (blocks > cap) blocks = cap > 0 ? cap : 1;
+  fn<<<(unsigned)blocks, kThreads, 0, st>>>(d_scenes, d_views, n_views, quarters, rgb, queue, status,
+                                            std::min(num_sms(), kMaxStrips));
   return cudaGetLastError();
 }
 

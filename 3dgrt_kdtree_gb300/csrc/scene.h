@@ -100,7 +100,7 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
                          const uint32_t totals[3], float* rgb, float* alpha, float* depth, uint32_t* queue,
                          cudaStream_t st);
 int batch_sms();
-// Multi-scene persistent launch (CTA-block schedule) for the serving loop;
+// Multi-scene persistent launch (warp-strip schedule) for the serving loop;
 // views[].scene indexes d_scenes.
 cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* d_views, int n_views,
                          uint32_t total_blocks, float* rgb, uint32_t* queue, uint32_t* status, cudaStream_t st);
