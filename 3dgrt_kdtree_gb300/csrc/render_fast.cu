@@ -664,7 +664,9 @@ __device__ __forceinline__ void pkt_trace(const FastView& S, Ray& R, bool live, 
         if (!pkt_leaf<K, PACKED>(S, base, cnt, R, part, status)) done = true;
         if (part) {
           t_done = R.t_far;
-          if (R.A > 0.99f || R.t_far >= R.t_scene_far) done = true;
+          // inside a leaf only A > 0.99 stops a ray; at a leaf boundary the
+          // walk goes on only while A < 0.99 (A == 0.99 stops here)
+          if (!(R.A < 0.99f) || R.t_far >= R.t_scene_far) done = true;
         }
       }
     }

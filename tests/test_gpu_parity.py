@@ -137,6 +137,37 @@ def test_1080p_1m_strided_rays_bit_exact(pkg, O, cuda, cluster_1m):
     assert (g_a > 0.99).mean() > 0.5
 
 
+def test_1080p_1m_fast_forms_full_size(pkg, O, cuda, cluster_1m):
+    """Full-size check of the batched forms on the 1M / 1080p workload: warp
+    packets and per-ray traversal give the same frame (every ray keeps its own
+    leaves and intervals), and every 97th ray of both forms is within the
+    1e-3 RMSE bar of the FP64 oracle."""
+    rec, tree = cluster_1m
+    F = pkg.renderer
+    W, H = 1920, 1080
+    cam = pkg.scenes.front_camera(W, H)
+    scene = F.Scene(tree, rec, forms=F.FORM_FAST | F.FORM_PACKED)
+    views, total, _ = F.make_views([(cam, W, H)])
+    pix = np.arange(0, W * H, 97, dtype=np.uint32)
+    r64, _, _, _ = oracle_image(O, tree, rec, cam, W, H, precision="f64", pixels=pix)
+    fi = flipped_index(pix.astype(np.int64), W, H)
+    for prec in (0, 1):
+        frames = []
+        for trav in (F.TRAV_PACKET, F.TRAV_RAY):
+            cfg = F.BatchConfig.default()
+            cfg.precision, cfg.traversal = prec, trav
+            rgb = torch.zeros(total * 3, device=cuda)
+            scene.render_batch(views, 1, rgb, cfg=cfg)
+            torch.cuda.synchronize()
+            frames.append(rgb.cpu().numpy())
+        assert float(np.abs(frames[0] - frames[1]).max()) <= 1e-5, prec
+        got = frames[0].reshape(-1, 3)[fi].astype(np.float64)
+        assert float(np.sqrt(((got - r64) ** 2).mean())) <= 1e-3, prec
+        assert np.isfinite(frames[0]).all() and (frames[0] >= 0).all()
+    assert scene.status() == 0
+    scene.close()
+
+
 def test_corrupt_tree_rejected_before_launch(pkg, cuda):
     t = pkg.kdtree.KdTree(np.array([[(5 << 3) | 0, 0], [3, 0], [3, 0]], np.uint32), np.zeros(0, np.uint32),
                           np.array([-1, -1, -1, 1, 1, 1], np.float32))
