@@ -53,7 +53,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     nvcc = os.path.join(cuda, "bin", "nvcc")
     inc = ["-I" + os.path.join(REPO, "include"), "-I" + CSRC]
     jobs = []
-    # KDGR_NVCC_DEFINES: extra -D options (e.g. "KDGR_FAST_HITS=2 KDGR_FAST_PIPE=1") for
+    # KDGR_NVCC_DEFINES: extra -D options (e.g. "KDGR_FAST_HITS=2 KDGR_FAST_STACK=16") for
     # compile-time variants of the fast kernel
     defs = ["-D" + d for d in os.environ.get("KDGR_NVCC_DEFINES", "").split()]
     for src, extra in CU_UNITS.items():
