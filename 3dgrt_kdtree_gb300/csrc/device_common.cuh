@@ -35,39 +35,44 @@ struct ExactView {
   float bmin[3], bmax[3];
 };
 
-// Device arrays of the fast forms.
+// Device arrays of one fast form (kdgr_scene_s::fast_view(packed)).
 //   nodes:      re-laid-out tree: the top levels breadth-first, the rest
 //               depth-first by subtree; children stay pairwise adjacent.
-//               Leaf words: x as in the file (count << 3 | 3), y = the
-//               leaf's first pair p; its entries are 2p .. 2p + count - 1,
-//               and an odd leaf ends with one padding entry;
-//   offsets:    Gaussian ID of every entry in that padded leaf order
-//               (0xFFFFFFFF for padding), read for accepted hits only;
-//               n_offsets counts the padded entries;
+//               Leaf words: x = count << 3 | 3, y = the leaf's first pair p
+//               of the main stream; its entries are 2p .. 2p + count - 1,
+//               and an odd count ends with one padding entry.  The packed
+//               form has its own leaf words: count and pairs cover only the
+//               leaf's plain entries;
+//   offsets:    Gaussian ID of every main-stream entry in that padded leaf
+//               order (0xFFFFFFFF for padding), read for accepted hits only;
+//               n_offsets counts them;
 //   opacity:    1 float per Gaussian;
 //   sh:         FP32 coefficient-major (shared with ExactView);
 //   sh_bf16:    6 x uint4 per Gaussian, BF16 coefficient-major;
-//   aniso_idx / aniso: for flagged Gaussians (scale ratio > 1e3, or factors
-//               beyond FP16), the index into 3 x float4 (M0,b0)(M1,b1)(M2,b2)
-//               from the FP64 upload precompute;
-//   leaf_pairs: FP32 form, per pair of leaf entries (2p, 2p+1) the rows of
-//               M = diag(1/s) R^T and b = M mu interleaved lo/hi, 6 x float4;
-//   leaf_packed: packed form, per pair of leaf entries 4 x uint4: the FP32
-//               means and the FP16 entries of M interleaved lo/hi, and a
-//               flag word (bit k: entry k reads the FP64-precomputed table);
-//   Padding entries hold zero records: M = 0 gives |grdu|^2 = 0 and
-//   t* = 0 * inf = NaN, which no leaf interval accepts.
+//   leaf_pairs: FP32 pairs: per pair of entries (2p, 2p+1) the rows of
+//               M = diag(1/s) R^T and b = M mu interleaved lo/hi, 6 x float4.
+//               The FP32 form's main stream; in the packed form the stream of
+//               flagged entries (scale ratio > 1e3, or factors beyond FP16),
+//               whose rows come from the FP64 upload precompute;
+//   leaf_packed: packed form, per pair of plain entries 4 x uint4: the FP32
+//               means and the FP16 entries of M interleaved lo/hi;
+//   leaf_aux:   packed form, per node: at a leaf (first flagged pair, number
+//               of flagged entries); flag_offsets their Gaussian IDs (n_flag).
+//   A leaf's hit index runs over its main-stream entries, then (packed) its
+//   flagged entries.  Padding entries hold zero records: M = 0 gives
+//   |grdu|^2 = 0 and t* = 0 * inf = NaN, which no leaf interval accepts.
 struct FastView {
   const uint2* nodes;
   const uint32_t* offsets;
   const float* opacity;
   const float4* sh;
   const uint4* sh_bf16;
-  const uint32_t* aniso_idx;
-  const float4* aniso;
-  const float4* leaf_pairs;  // FP32 test records in leaf order, interleaved pairs (6 x float4 per pair)
-  const uint4* leaf_packed;  // packed records in leaf order
-  uint32_t n_nodes, n_offsets, n_gauss, top_nodes;
+  const float4* leaf_pairs;     // FP32 pairs (6 x float4): the FP32 form's leaf entries, or the
+                                //   packed form's flagged entries
+  const uint4* leaf_packed;     // packed form: FP16 pairs of the plain entries
+  const uint2* leaf_aux;        // packed form, per node: (first flagged pair, n_flagged) at leaves
+  const uint32_t* flag_offsets; // packed form: Gaussian of every padded flagged entry
+  uint32_t n_nodes, n_offsets, n_flag, n_gauss, top_nodes;
   float bmin[3], bmax[3];
 };
 

@@ -141,19 +141,20 @@ kdgr::ExactView kdgr_scene_s::exact_view() const {
   return v;
 }
 
-kdgr::FastView kdgr_scene_s::fast_view() const {
+kdgr::FastView kdgr_scene_s::fast_view(bool packed) const {
   FastView v;
-  v.nodes = d_nodes_fast;
-  v.offsets = d_pair_gid;
+  v.nodes = packed ? d_nodes_packed : d_nodes_fast;
+  v.offsets = packed ? d_gid_plain : d_pair_gid;
   v.opacity = d_opacity;
   v.sh = d_sh;
   v.sh_bf16 = d_sh_bf16;
-  v.aniso_idx = d_aniso_idx;
-  v.aniso = d_aniso;
-  v.leaf_pairs = d_leaf_pairs;
+  v.leaf_pairs = packed ? d_flag_pairs : d_leaf_pairs;
   v.leaf_packed = d_leaf_packed;
+  v.leaf_aux = packed ? d_leaf_aux : nullptr;
+  v.flag_offsets = packed ? d_gid_flag : nullptr;
   v.n_nodes = n_nodes;
-  v.n_offsets = n_pair_entries;
+  v.n_offsets = packed ? n_plain_entries : n_pair_entries;
+  v.n_flag = packed ? n_flag_entries : 0u;
   v.n_gauss = n_gauss;
   v.top_nodes = top_nodes;
   for (int i = 0; i < 3; ++i) {
@@ -291,8 +292,8 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
         cudaMemcpy(s->d_test, te.data(), te.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
       return fail("kdgr_scene_create: upload (exact)");
   }
+  std::vector<uint32_t> relaid, pair_gid;  // relaid fast tree, padded leaf order (fast forms)
   if (forms & (KDGR_FORM_FAST | KDGR_FORM_PACKED)) {
-    std::vector<uint32_t> relaid, pair_gid;
     relayout_tree(nodes, n_nodes, kTopLevels, relaid, &s->top_nodes);
     pad_leaf_pairs(relaid, offsets, pair_gid);
     if (pair_gid.size() > 0xFFFFFFF0ull) {
@@ -342,7 +343,7 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
     if (e != cudaSuccess) return fail("kdgr_scene_create: upload (fast)");
   }
   if (forms & KDGR_FORM_PACKED) {
-    rc = pack_precision(s.get(), g, giscl.data(), sh.data(), A);
+    rc = pack_precision(s.get(), g, giscl.data(), sh.data(), relaid, pair_gid, A);
     if (rc != KDGR_OK) {
       A.release();
       return rc;
@@ -357,8 +358,9 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
 int kdgr_scene_destroy(kdgr_scene_t s) {
   if (!s) return KDGR_ERR_INVALID_ARG;
   void* ps[] = {s->d_nodes,     s->d_offsets, s->d_test,      s->d_sh,          s->d_nodes_fast,
-                s->d_opacity,   s->d_sh_bf16,     s->d_aniso_idx,
-                s->d_aniso,     s->d_leaf_pairs, s->d_leaf_packed, s->d_pair_gid, s->d_status};
+                s->d_opacity,   s->d_sh_bf16,     s->d_leaf_pairs,  s->d_leaf_packed, s->d_pair_gid,
+                s->d_nodes_packed, s->d_leaf_aux, s->d_gid_plain, s->d_gid_flag, s->d_flag_pairs,
+                s->d_status};
   cudaError_t first = cudaSuccess;
   for (void* p : ps)
     if (p) {

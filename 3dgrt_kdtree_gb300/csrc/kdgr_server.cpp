@@ -384,7 +384,7 @@ int kdgr_server_add_scene(kdgr_server_t s, const uint32_t* nodes, uint32_t n_nod
     set_error("kdgr_server_add_scene: scene exceeds the HBM budget");
     return KDGR_ERR_BUDGET;
   }
-  const FastView fv = sc->fast_view();
+  const FastView fv = sc->fast_view(s->cfg.precision != 0);
   cudaError_t e = cudaMemcpy(s->d_scenes + slot, &fv, sizeof(FastView), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     kdgr_scene_destroy(sc);

@@ -208,9 +208,8 @@ struct PPairRec {
 
 // Packed pair: FP16 rows of M, FP32 mean, ng = M (mu - o) (no M o - M mu
 // cancellation, so the FP16 rounding stays a small consistent perturbation
-// of the Gaussian); flagged entries take the FP64-precomputed factors.
-__device__ __forceinline__ void setup_ppair(const FastView& S, const PPairRec& r, const Ray2& w, F3 o, F3 d,
-                                            PairT& p) {
+// of the Gaussian).
+__device__ __forceinline__ void setup_ppair(const PPairRec& r, const Ray2& w, PairT& p) {
   const f2 nqx = add2(u2f2(r.w[0].x, r.w[0].y), w.nox);
   const f2 nqy = add2(u2f2(r.w[0].z, r.w[0].w), w.noy);
   const f2 nqz = add2(u2f2(r.w[1].x, r.w[1].y), w.noz);
@@ -220,27 +219,6 @@ __device__ __forceinline__ void setup_ppair(const FastView& S, const PPairRec& r
     const f2 m0 = h2f2(mw[3 * i]), m1 = h2f2(mw[3 * i + 1]), m2 = h2f2(mw[3 * i + 2]);
     p.ng[i] = fma2(m0, nqx, fma2(m1, nqy, mul2(m2, nqz)));
     p.gd[i] = fma2(m0, w.dx, fma2(m1, w.dy, mul2(m2, w.dz)));
-  }
-  const uint32_t fl = r.w[3].w;
-  if (fl) {
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      if (!((fl >> k) & 1u)) continue;
-      // a flagged entry's mean.x slot holds its index into the FP64 table
-      const float4* t = S.aniso + 3ull * (k ? r.w[0].y : r.w[0].x);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const float4 row = __ldg(t + i);
-        const F3 m = mk(row.x, row.y, row.z);
-        const float ng = row.w - dot3(m, o), gd = dot3(m, d);
-        // replace lane k with integer masks (a split2/join2 round trip with
-        // one half replaced did not store the new half)
-        const unsigned long long sh = k ? 32ull : 0ull;
-        const unsigned long long mask = 0xFFFFFFFFull << sh;
-        p.ng[i] = (p.ng[i] & ~mask) | ((unsigned long long)__float_as_uint(ng) << sh);
-        p.gd[i] = (p.gd[i] & ~mask) | ((unsigned long long)__float_as_uint(gd) << sh);
-      }
-    }
   }
 }
 
@@ -252,16 +230,45 @@ __device__ __forceinline__ PPairRec load_ppair(const FastView& S, uint32_t p) {
   return r;
 }
 
-// The t* step for pair `pair` of either form.
+// A leaf of either form: `np` pairs of the main stream from pair `pb`
+// (FP32 pairs, or packed FP16 pairs), then in the packed form `nf` FP32
+// pairs of its flagged entries from pair `fb` (leaf_pairs holds that stream).
+struct LeafRef {
+  uint32_t pb, np, fb, nf;
+};
+
 template <bool PACKED>
-__device__ __forceinline__ unsigned test_pair_t(const FastView& S, uint32_t pair, const Ray2& w, F3 o, F3 d,
-                                                float t_near, float t_far, PairT& p) {
+__device__ __forceinline__ LeafRef leaf_ref(const FastView& S, uint32_t node, uint2 nd) {
+  LeafRef L{nd.y, ((nd.x >> 3) + 1) >> 1, 0u, 0u};
   if constexpr (PACKED) {
-    setup_ppair(S, load_ppair(S, pair), w, o, d, p);
+    const uint2 a = __ldg(S.leaf_aux + node);
+    L.fb = a.x;
+    L.nf = (a.y + 1) >> 1;
+  }
+  return L;
+}
+
+__device__ __forceinline__ bool leaf_in_bounds(const FastView& S, const LeafRef& L) {
+  return 2ull * ((uint64_t)L.pb + L.np) <= S.n_offsets && 2ull * ((uint64_t)L.fb + L.nf) <= S.n_flag;
+}
+
+// The t* step for pair j of leaf L.
+template <bool PACKED>
+__device__ __forceinline__ unsigned leaf_pair_t(const FastView& S, const LeafRef& L, uint32_t j, const Ray2& w,
+                                                float t_near, float t_far, PairT& p) {
+  if (PACKED && j < L.np) {
+    setup_ppair(load_ppair(S, L.pb + j), w, p);
   } else {
-    setup_pair(load_pair(S, pair), w, p);
+    setup_pair(load_pair(S, PACKED ? L.fb + (j - L.np) : L.pb + j), w, p);
   }
   return pair_t(p, t_near, t_far);
+}
+
+// Gaussian of leaf entry ik.
+template <bool PACKED>
+__device__ __forceinline__ uint32_t leaf_gid(const FastView& S, const LeafRef& L, uint32_t ik) {
+  if (PACKED && ik >= 2 * L.np) return __ldg(S.flag_offsets + 2 * L.fb + (ik - 2 * L.np));
+  return __ldg(S.offsets + 2 * L.pb + ik);
 }
 
 __device__ __forceinline__ unsigned test_pair_g(const PairT& p, unsigned m, float t[2], float g[2]) {
@@ -453,8 +460,8 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     R.cur = idx;
     nd = __ldg(S.nodes + R.cur);
   }
-  const uint32_t cnt = nd.x >> 3, pb = nd.y, base = 2 * pb;  // first pair, first entry
-  if ((uint64_t)base + cnt > S.n_offsets) {
+  const LeafRef L = leaf_ref<PACKED>(S, R.cur, nd);
+  if (!leaf_in_bounds(S, L)) {
     atomicOr(status, kStatusBadLeaf);
     return true;
   }
@@ -466,12 +473,11 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
     hb.clear();
     bool overflow = false;
     {
-      const uint32_t np = (cnt + 1) >> 1;
       const Ray2 w = ray2(R.o, R.d);
-      for (uint32_t p = 0; p < np; ++p) {
+      for (uint32_t p = 0; p < L.np + L.nf; ++p) {
         float t2[2], g2[2];
         PairT pt;
-        unsigned m = test_pair_t<PACKED>(S, pb + p, w, R.o, R.d, R.t_near, R.t_far, pt);  // padding never passes
+        unsigned m = leaf_pair_t<PACKED>(S, L, p, w, R.t_near, R.t_far, pt);  // padding never passes
         if (m) {
           m = test_pair_g(pt, m, t2, g2);
 #pragma unroll
@@ -486,7 +492,7 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       if (hb.t[k] == __int_as_float(0x7f800000)) break;
-      const uint32_t gid = __ldg(S.offsets + base + hb.i[k]);
+      const uint32_t gid = leaf_gid<PACKED>(S, L, hb.i[k]);
       if (gid >= S.n_gauss) {
         atomicOr(status, kStatusBadId);
         return true;
@@ -547,26 +553,24 @@ struct PktEnt {
 // Leaf [base, base + cnt) for the lanes with part set; every lane runs the
 // same candidate loop.  Returns false on a bad Gaussian ID (status set).
 template <int K, bool PACKED>
-__device__ __forceinline__ bool pkt_leaf(const FastView& S, uint32_t base, uint32_t cnt, Ray& R, bool part,
+__device__ __forceinline__ bool pkt_leaf(const FastView& S, const LeafRef& L, Ray& R, bool part,
                                          uint32_t* status) {
   const float kInf = __int_as_float(0x7f800000);
   bool have_last = false, ok = true;
   float last_t = 0.f;
   uint32_t last_i = 0;
   bool more = part;
-  const uint32_t pb = base >> 1;
   while (__any_sync(0xFFFFFFFFu, more)) {
     HitBuf<K> hb;
     hb.clear();
     bool overflow = false;
     const float tn = more ? R.t_near : kInf;
     {
-      const uint32_t np = (cnt + 1) >> 1;
       const Ray2 w = ray2(R.o, R.d);
-      for (uint32_t p = 0; p < np; ++p) {
+      for (uint32_t p = 0; p < L.np + L.nf; ++p) {
         float t2[2], g2[2];
         PairT pt;
-        unsigned m = test_pair_t<PACKED>(S, pb + p, w, R.o, R.d, tn, R.t_far, pt);  // padding never passes
+        unsigned m = leaf_pair_t<PACKED>(S, L, p, w, tn, R.t_far, pt);  // padding never passes
         // warp-uniform branches: most pairs have no lane with t* in range
         if (__any_sync(0xFFFFFFFFu, m != 0u)) {
           m = test_pair_g(pt, m, t2, g2);
@@ -584,7 +588,7 @@ __device__ __forceinline__ bool pkt_leaf(const FastView& S, uint32_t base, uint3
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       if (hb.t[k] == kInf || R.A > 0.99f) break;
-      const uint32_t gid = __ldg(S.offsets + base + hb.i[k]);
+      const uint32_t gid = leaf_gid<PACKED>(S, L, hb.i[k]);
       if (gid >= S.n_gauss) {
         atomicOr(status, kStatusBadId);
         ok = false;
@@ -654,14 +658,14 @@ __device__ __forceinline__ void pkt_trace(const FastView& S, Ray& R, bool live, 
       nd = __ldg(S.nodes + cur);
     }
     if (leaf) {
-      const uint32_t cnt = nd.x >> 3, base = 2 * nd.y;  // first entry of the leaf's first pair
-      if ((uint64_t)base + cnt > S.n_offsets) {
+      const LeafRef L = leaf_ref<PACKED>(S, cur, nd);
+      if (!leaf_in_bounds(S, L)) {
         if ((tid & 31) == 0) atomicOr(status, kStatusBadLeaf);
         break;
       }
       const bool part = act && !done;
       if (__any_sync(full, part)) {
-        if (!pkt_leaf<K, PACKED>(S, base, cnt, R, part, status)) done = true;
+        if (!pkt_leaf<K, PACKED>(S, L, R, part, status)) done = true;
         if (part) {
           t_done = R.t_far;
           // inside a leaf only A > 0.99 stops a ray; at a leaf boundary the
@@ -1127,13 +1131,13 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
   const uint64_t grabs = strips ? total : ((uint64_t)total + chunk - 1) / chunk;
   const uint64_t cap = per_warp ? (grabs + kWarps - 1) / kWarps : grabs;
   if (blocks > cap) blocks = cap > 0 ? cap : 1;
-  fn<<<(unsigned)blocks, kThreads, 0, st>>>(s->fast_view(), d_views, n_views, total, rgb, alpha, depth, queue,
-                                            s->d_status, chunk,
-                                            c.tile_shape);
+  fn<<<(unsigned)blocks, kThreads, 0, st>>>(s->fast_view(c.precision != 0), d_views, n_views, total, rgb, alpha,
+                                            depth, queue, s->d_status, chunk, c.tile_shape);
   return cudaGetLastError();
 }
 
-int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh, DevAlloc& A) {
+int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh,
+                   const std::vector<uint32_t>& relaid, const std::vector<uint32_t>& pair_gid, DevAlloc& A) {
   const size_t n = s->n_gauss;
   std::vector<uint32_t> packed(8 * n);
   std::vector<uint16_t> shb(48 * n);
@@ -1174,7 +1178,7 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
     memcpy(&p[0], &r[0], 4);
     memcpy(&p[1], &r[1], 4);
     memcpy(&p[2], &r[2], 4);
-    p[3] = pk(m[2][2], aniso ? 1.f : 0.f);
+    p[3] = pk(m[2][2], 0.f);
     p[4] = pk(m[0][0], m[0][1]);
     p[5] = pk(m[0][2], m[1][0]);
     p[6] = pk(m[1][1], m[1][2]);
@@ -1196,45 +1200,86 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
         cudaMemcpy(s->d_opacity, opac.data(), n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
       return cuda_fail(cudaErrorUnknown, "kdgr_scene_create: opacity upload (packed)");
   }
-  uint4* d_stage = nullptr;  // per-Gaussian packed records: staging for the leaf-order copy
+  // The packed form's leaf layout: per leaf its plain entries in FP16 pairs,
+  // then its flagged entries in FP32 pairs of a second stream, both padded
+  // to whole pairs; the leaf words and per-node aux words say where.
+  std::vector<uint32_t> nodes_p(relaid), gid_plain, gid_flag;
+  std::vector<uint32_t> aux(relaid.size(), 0u);
+  std::vector<uint32_t> plain, flagged;
+  for (size_t nd = 0; 2 * nd < relaid.size(); ++nd) {
+    const uint32_t x = relaid[2 * nd];
+    if ((x & 7u) != 3u) continue;
+    const uint32_t cnt = x >> 3, e0 = 2 * relaid[2 * nd + 1];
+    plain.clear();
+    flagged.clear();
+    for (uint32_t k = 0; k < cnt; ++k) {
+      const uint32_t gid = pair_gid[e0 + k];
+      (aidx[gid] == 0xFFFFFFFFu ? plain : flagged).push_back(gid);
+    }
+    nodes_p[2 * nd] = ((uint32_t)plain.size() << 3) | 3u;
+    nodes_p[2 * nd + 1] = (uint32_t)(gid_plain.size() / 2);
+    aux[2 * nd] = (uint32_t)(gid_flag.size() / 2);
+    aux[2 * nd + 1] = (uint32_t)flagged.size();
+    gid_plain.insert(gid_plain.end(), plain.begin(), plain.end());
+    if (plain.size() & 1u) gid_plain.push_back(kPadGid);
+    gid_flag.insert(gid_flag.end(), flagged.begin(), flagged.end());
+    if (flagged.size() & 1u) gid_flag.push_back(kPadGid);
+  }
+  if (gid_plain.size() > 0xFFFFFFF0ull || gid_flag.size() > 0xFFFFFFF0ull) {
+    set_error("kdgr_scene_create: more than 2^32 leaf entries after pair padding");
+    return KDGR_ERR_LIMIT;
+  }
+  s->n_plain_entries = (uint32_t)gid_plain.size();
+  s->n_flag_entries = (uint32_t)gid_flag.size();
+  s->n_aniso = n_aniso;
   s->d_sh_bf16 = A.alloc<uint4>(6 * n);
-  s->d_aniso_idx = A.alloc<uint32_t>(n);
-  s->d_aniso = A.alloc<float4>(3 * (size_t)(n_aniso ? n_aniso : 1));
-  float* d_src = nullptr;
+  s->d_nodes_packed = A.alloc<uint2>(relaid.size() / 2);
+  s->d_leaf_aux = A.alloc<uint2>(relaid.size() / 2);
+  s->d_gid_plain = A.alloc<uint32_t>(gid_plain.size() + 2);
+  s->d_gid_flag = A.alloc<uint32_t>(gid_flag.size() + 2);
+  s->d_leaf_packed = A.alloc<uint4>(2 * (gid_plain.size() + 2));
+  s->d_flag_pairs = A.alloc<float4>(3 * (gid_flag.size() + 2));
   if (A.err != cudaSuccess) return cuda_fail(A.err, "kdgr_scene_create: cudaMalloc (packed)");
+  // staging: per-Gaussian packed words, aniso index, FP64 precompute
+  uint32_t *d_stage = nullptr, *d_aidx = nullptr;
+  float* d_src = nullptr;
+  float4* d_table = nullptr;
+  auto up = [](void* dst, const void* src, size_t bytes) {
+    return bytes ? cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+  };
   cudaError_t e = cudaMalloc(&d_stage, packed.size() * 4);
-  if (e == cudaSuccess) e = cudaMemcpy(d_stage, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(s->d_sh_bf16, shb.data(), shb.size() * 2, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(s->d_aniso_idx, aidx.data(), aidx.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = up(d_stage, packed.data(), packed.size() * 4);
+  if (e == cudaSuccess) e = up(s->d_sh_bf16, shb.data(), shb.size() * 2);
+  if (e == cudaSuccess) e = up(s->d_nodes_packed, nodes_p.data(), nodes_p.size() * 4);
+  if (e == cudaSuccess) e = up(s->d_leaf_aux, aux.data(), aux.size() * 4);
+  if (e == cudaSuccess) e = up(s->d_gid_plain, gid_plain.data(), gid_plain.size() * 4);
+  if (e == cudaSuccess) e = up(s->d_gid_flag, gid_flag.data(), gid_flag.size() * 4);
+  if (e == cudaSuccess) e = build_packed_pairs(s->d_gid_plain, s->n_plain_entries, d_stage, s->d_leaf_packed);
   if (e == cudaSuccess && n_aniso) {
     e = cudaMalloc(&d_src, aniso_src.size() * 4);
-    if (e == cudaSuccess) e = cudaMemcpy(d_src, aniso_src.data(), aniso_src.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&d_table, 3 * sizeof(float4) * n_aniso);
+    if (e == cudaSuccess) e = cudaMalloc(&d_aidx, aidx.size() * 4);
+    if (e == cudaSuccess) e = up(d_src, aniso_src.data(), aniso_src.size() * 4);
+    if (e == cudaSuccess) e = up(d_aidx, aidx.data(), aidx.size() * 4);
     if (e == cudaSuccess) {
-      k_aniso_fp64<<<(n_aniso + 127) / 128, 128>>>(d_src, n_aniso, s->d_aniso);
+      k_aniso_fp64<<<(n_aniso + 127) / 128, 128>>>(d_src, n_aniso, d_table);
       e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    if (d_src) cudaFree(d_src);
+    if (e == cudaSuccess) e = build_flag_pairs(s->d_gid_flag, s->n_flag_entries, d_aidx, d_table, s->d_flag_pairs);
   }
-  if (e == cudaSuccess) {
-    s->n_aniso = n_aniso;
-    s->d_leaf_packed = A.alloc<uint4>(2 * ((size_t)s->n_pair_entries + 2));
-    e = A.err;
-  }
-  if (e == cudaSuccess)
-    e = build_packed_pairs(s->d_pair_gid, s->n_pair_entries, reinterpret_cast<const uint32_t*>(d_stage),
-                           s->d_aniso_idx, s->d_leaf_packed);
-  if (d_stage) cudaFree(d_stage);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  for (void* q : {(void*)d_stage, (void*)d_src, (void*)d_table, (void*)d_aidx})
+    if (q) cudaFree(q);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed upload");
   return KDGR_OK;
 }
 
-// Pair p of the packed leaf records (layout at PPairRec) from the
-// per-Gaussian staging words: mean x, y, z (FP32), half2 (M22, flag),
+// Pair p of the packed plain records (layout at PPairRec) from the
+// per-Gaussian staging words: mean x, y, z (FP32), half2 (M22, 0),
 // half2 (M00, M01), (M02, M10), (M11, M12), (M20, M21).  Padding entries
-// are zero; a flagged entry's mean.x becomes its FP64-table index.
+// are zero.
 __global__ void k_build_ppairs(const uint32_t* __restrict__ gid, uint32_t n, const uint32_t* __restrict__ src,
-                               const uint32_t* __restrict__ aniso_idx, uint4* __restrict__ out) {
+                               uint4* __restrict__ out) {
   const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= (size_t)n / 2) return;
   uint32_t a[8], b[8];
@@ -1247,15 +1292,29 @@ __global__ void k_build_ppairs(const uint32_t* __restrict__ gid, uint32_t n, con
   auto lo = [](uint32_t x) { return x & 0xFFFFu; };
   auto hi = [](uint32_t x) { return x >> 16; };
   auto h2 = [](uint32_t l, uint32_t h) { return l | (h << 16); };
-  // flagged entries carry their FP64-table index in place of mean.x
-  if (hi(a[3]) != 0u) a[0] = __ldg(aniso_idx + g0);
-  if (hi(b[3]) != 0u) b[0] = __ldg(aniso_idx + g1);
   out[4 * p] = make_uint4(a[0], b[0], a[1], b[1]);
   out[4 * p + 1] = make_uint4(a[2], b[2], h2(lo(a[4]), lo(b[4])), h2(hi(a[4]), hi(b[4])));
   out[4 * p + 2] = make_uint4(h2(lo(a[5]), lo(b[5])), h2(hi(a[5]), hi(b[5])), h2(lo(a[6]), lo(b[6])),
                               h2(hi(a[6]), hi(b[6])));
-  out[4 * p + 3] = make_uint4(h2(lo(a[7]), lo(b[7])), h2(hi(a[7]), hi(b[7])), h2(lo(a[3]), lo(b[3])),
-                              (hi(a[3]) != 0u ? 1u : 0u) | (hi(b[3]) != 0u ? 2u : 0u));
+  out[4 * p + 3] = make_uint4(h2(lo(a[7]), lo(b[7])), h2(hi(a[7]), hi(b[7])), h2(lo(a[3]), lo(b[3])), 0u);
+}
+
+// Pair p of the packed form's flagged stream, in the FP32 pair layout, from
+// the FP64-precomputed rows (M row i, b_i) of Gaussian-order table entry
+// aidx[gid]; padding entries are zero.
+__global__ void k_build_flag_pairs(const uint32_t* __restrict__ gid, uint32_t n, const uint32_t* __restrict__ aidx,
+                                   const float4* __restrict__ table, float4* __restrict__ pairs) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (size_t)n / 2) return;
+  const uint32_t g0 = __ldg(gid + 2 * p), g1 = __ldg(gid + 2 * p + 1);
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float4 a = g0 == kPadGid ? z : __ldg(table + 3ull * __ldg(aidx + g0) + i);
+    const float4 b = g1 == kPadGid ? z : __ldg(table + 3ull * __ldg(aidx + g1) + i);
+    pairs[6 * p + 2 * i] = make_float4(a.x, b.x, a.y, b.y);
+    pairs[6 * p + 2 * i + 1] = make_float4(a.z, b.z, a.w, b.w);
+  }
 }
 
 // Pair p of the FP32 leaf records: entries 2p and 2p+1, rows of M and b
@@ -1284,14 +1343,19 @@ cudaError_t build_leaf_pairs(const uint32_t* d_gid, uint32_t n_entries, const fl
   return e;
 }
 
-cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src,
-                               const uint32_t* aniso_idx, uint4* pairs) {
+cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src, uint4* pairs) {
   if (n_entries == 0) return cudaSuccess;
   const size_t np = (size_t)n_entries / 2;
-  k_build_ppairs<<<(unsigned)((np + 255) / 256), 256>>>(d_gid, n_entries, src, aniso_idx, pairs);
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaDeviceSynchronize();
-  return e;
+  k_build_ppairs<<<(unsigned)((np + 255) / 256), 256>>>(d_gid, n_entries, src, pairs);
+  return cudaGetLastError();
+}
+
+cudaError_t build_flag_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* aidx, const float4* table,
+                             float4* pairs) {
+  if (n_entries == 0) return cudaSuccess;
+  const size_t np = (size_t)n_entries / 2;
+  k_build_flag_pairs<<<(unsigned)((np + 255) / 256), 256>>>(d_gid, n_entries, aidx, table, pairs);
+  return cudaGetLastError();
 }
 
 int batch_sms() { return num_sms(); }

@@ -26,8 +26,6 @@ struct kdgr_scene_s {
   uint32_t top_nodes = 0;
   float* d_opacity = nullptr;
   uint4* d_sh_bf16 = nullptr;
-  uint32_t* d_aniso_idx = nullptr;
-  float4* d_aniso = nullptr;
   // leaf-major copies of the test records, padded per leaf to whole pairs:
   // the fast tree's leaf word y is the leaf's first pair p, its entries are
   // 2p .. 2p+cnt-1 and an odd leaf ends with one padding entry;
@@ -36,7 +34,16 @@ struct kdgr_scene_s {
   uint32_t* d_pair_gid = nullptr;
   uint32_t n_pair_entries = 0;     // even
   float4* d_leaf_pairs = nullptr;  // FP32 form, 6 x float4 per pair of entries
-  uint4* d_leaf_packed = nullptr;  // packed form, 4 x uint4 per pair of entries
+  uint4* d_leaf_packed = nullptr;  // packed form, 4 x uint4 per pair of plain entries
+  // The packed form's own leaf layout: a leaf's plain entries in FP16 pairs
+  // (d_leaf_packed), its flagged entries (scale ratio > 1e3 or factors beyond
+  // FP16: FP64-precomputed factors) in FP32 pairs of a second stream.
+  uint2* d_nodes_packed = nullptr;  // leaf words (n_plain << 3 | 3, first plain pair)
+  uint2* d_leaf_aux = nullptr;      // per node; at leaves (first flagged pair, n_flagged)
+  uint32_t* d_gid_plain = nullptr;  // Gaussian of every padded plain entry
+  uint32_t* d_gid_flag = nullptr;   // Gaussian of every padded flagged entry
+  float4* d_flag_pairs = nullptr;   // 6 x float4 per flagged pair (FP32 pair layout)
+  uint32_t n_plain_entries = 0, n_flag_entries = 0;
   uint32_t n_aniso = 0;
   // per-scene status word written by kernels (error bits)
   uint32_t* d_status = nullptr;
@@ -44,7 +51,7 @@ struct kdgr_scene_s {
   std::mutex mu;
 
   kdgr::ExactView exact_view() const;
-  kdgr::FastView fast_view() const;
+  kdgr::FastView fast_view(bool packed) const;
 };
 
 namespace kdgr {
@@ -76,17 +83,20 @@ void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std:
                    uint32_t* top_count);
 // Packed precision form: BF16 SH, FP16 inverse scales / quaternion /
 // opacity, and the FP64 upload-time factors of anisotropic Gaussians.
-int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh, DevAlloc& A);
+int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh,
+                   const std::vector<uint32_t>& relaid, const std::vector<uint32_t>& pair_gid, DevAlloc& A);
 // Fast-form leaf layout: rewrites the leaf words of the relaid tree
 // (y = first pair) and returns the padded per-entry Gaussian IDs.
 void pad_leaf_pairs(std::vector<uint32_t>& relaid, const uint32_t* offsets, std::vector<uint32_t>& pair_gid);
 constexpr uint32_t kPadGid = 0xFFFFFFFFu;
 // Pair records in padded leaf order (entry j = Gaussian gid[j], zero for
 // padding): FP32 from 3 float4 per Gaussian (rows of M and b), packed from
-// 8 words per Gaussian.
+// 8 words per Gaussian, flagged FP32 pairs from the FP64-precomputed table
+// (entry aidx[gid]).  The packed builders do not synchronize.
 cudaError_t build_leaf_pairs(const uint32_t* d_gid, uint32_t n_entries, const float4* test, float4* pairs);
-cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src,
-                               const uint32_t* aniso_idx, uint4* pairs);
+cudaError_t build_packed_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* src, uint4* pairs);
+cudaError_t build_flag_pairs(const uint32_t* d_gid, uint32_t n_entries, const uint32_t* aidx, const float4* table,
+                             float4* pairs);
 // Batched rendering (render_fast.cu).
 // totals: 8x4 tiles, 16x8 blocks and 32x16 super-blocks over all views.
 int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]);
