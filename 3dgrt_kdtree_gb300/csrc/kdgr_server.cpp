@@ -282,10 +282,15 @@ void kdgr_server_s::completer() {
 }
 
 static uint64_t estimate_scene_bytes(uint32_t n_nodes, uint32_t n_offsets, uint32_t n, bool packed) {
-  const uint64_t per = packed ? (96 + 4 + 4) : (4 + 192);  // SH, opacity (+ aniso index)
-  // ID, padded-order ID and leaf-order record; each leaf may add one padding entry
-  const uint64_t per_entry = 8 + (packed ? 32 : 48);
-  return 16ull * n_nodes + per_entry * (n_offsets + n_nodes / 2 + 1) + per * n;
+  const uint64_t per = packed ? (96 + 4) : (4 + 192);  // SH, opacity
+  // ID, padded-order ID and leaf-order record (packed: plus an allowance of
+  // 8 B per entry for the FP32 pairs of flagged entries, which hold about
+  // 1 entry in 10 in the cluster scenes); each leaf may add one padding
+  // entry.  Nodes: exact and fast trees, plus the packed form's leaf and aux
+  // words.  The exact bytes are checked after creation.
+  const uint64_t per_entry = 8 + (packed ? 32 + 8 : 48);
+  const uint64_t per_node = packed ? 32 : 16;
+  return per_node * n_nodes + per_entry * (n_offsets + n_nodes / 2 + 1) + per * n;
 }
 
 extern "C" {
