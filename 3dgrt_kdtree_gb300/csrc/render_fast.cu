@@ -550,8 +550,10 @@ struct PktEnt {
   uint32_t node, mask;
 };
 
-// Leaf [base, base + cnt) for the lanes with part set; every lane runs the
-// same candidate loop.  Returns false on a bad Gaussian ID (status set).
+// Leaf L for the lanes with part set; every lane runs the same candidate
+// loop (lanes without part test against an empty interval).  Inside the leaf
+// a ray stops compositing once A > 0.99.  Returns false on a bad Gaussian ID
+// (status set).
 template <int K, bool PACKED>
 __device__ __forceinline__ bool pkt_leaf(const FastView& S, const LeafRef& L, Ray& R, bool part,
                                          uint32_t* status) {
