@@ -110,6 +110,30 @@ def big_leaf(n=100, seed=7):
     return tree, rec, sc.front_camera(16, 16, fovy=6.0)
 
 
+def mixed_aniso(n=41, seed=11):
+    """Two leaves split at z = 0: the front leaf mixes n Gaussians of which
+    every third is very thin (scale ratio 2000, so the precision form reads
+    its FP64-precomputed factors), the back leaf holds only thin ones; odd
+    counts in both, so both of the precision form's pair streams end on a
+    padding entry."""
+    rng = np.random.default_rng(seed)
+    front, back = [], []
+    for i in range(n):
+        q = rng.normal(0, 1, 4)
+        thin = i % 3 == 0
+        s = (0.08, 0.06, 0.00004) if thin else (0.05, 0.04, 0.03)
+        front.append(gaussian((rng.normal(0, 0.03), rng.normal(0, 0.03), rng.uniform(0.05, 0.7)), s, quat=q,
+                              opacity=0.3, dc=rng.normal(0.5, 0.2, 3)))
+    for i in range(7):
+        q = rng.normal(0, 1, 4)
+        back.append(gaussian((rng.normal(0, 0.03), rng.normal(0, 0.03), rng.uniform(-0.7, -0.05)),
+                             (0.07, 0.05, 0.00003), quat=q, opacity=0.4, dc=rng.normal(0.5, 0.2, 3)))
+    gs = front + back
+    nodes = [inner(2, 1, 0.0), leaf(len(back), len(front)), leaf(len(front), 0)]
+    tree = make_tree(nodes, list(range(len(gs))), (-1, -1, -1, 1, 1, 1))
+    return tree, np.stack(gs), sc.front_camera(16, 16, fovy=6.0)
+
+
 def empty():
     g = gaussian((0.0, 0.0, 0.0), (0.1, 0.1, 0.1))
     tree = make_tree([leaf(0, 0)], [], (-1, -1, -1, 1, 1, 1))

@@ -158,6 +158,7 @@ KAT_CASES = {
     "big_leaf": lambda kat: (kat.big_leaf(100), 16, 16),
     "empty": lambda kat: (kat.empty(), 8, 8),
     "miss": lambda kat: (kat.miss(), 8, 8),
+    "mixed_aniso": lambda kat: (kat.mixed_aniso(), 16, 16),
 }
 
 
@@ -166,9 +167,10 @@ def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
     """The batching and precision forms on the hand-built scenes: a stack
     deeper than the ring (restarts), 20 equal-t hits in one leaf (more than
     the hit buffer: re-scan passes), a 100-candidate leaf, a Gaussian across
-    a split, an empty scene and a missed box; both within the accuracy bar
-    of the FP64 oracle, and the FP32 form equal across every schedule and
-    both traversals."""
+    a split, an empty scene, a missed box, and leaves mixing very thin
+    Gaussians (the precision form's FP32 stream) with plain ones; both forms
+    within the accuracy bar of the FP64 oracle and equal across every
+    schedule, tile shape and both traversals."""
     import kat
     (tree, rec, cam), W, H = KAT_CASES[case](kat)
     F = pkg.renderer
@@ -179,13 +181,16 @@ def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
         assert rmse(rgb, r64) <= RMSE_TOL, (prec, rmse(rgb, r64))
         assert rmse(a, a64) <= RMSE_TOL
     views, total, _ = F.make_views([(cam, W, H)])
-    ref = torch.zeros(total * 3, device=cuda)
-    scene.render_batch(views, 1, ref)
-    for sched, kb, trav, tile in [(0, 4, 0, 0), (1, 8, 0, 1), (2, 4, 0, 2), (3, 4, 0, 1), (0, 4, 1, 0),
-                                  (1, 8, 1, 2), (3, 8, 1, 0)]:
-        out = torch.full_like(ref, -1.0)
-        scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, 0, kb, trav, tile))
-        torch.cuda.synchronize()
-        np.testing.assert_array_equal(out.cpu().numpy(), ref.cpu().numpy())
+    if case == "mixed_aniso":
+        assert scene.info()["n_aniso"] == 21  # 14 thin in the front leaf, 7 in the back
+    for prec in (0, 1):
+        ref = torch.zeros(total * 3, device=cuda)
+        scene.render_batch(views, 1, ref, cfg=F.BatchConfig(1, 8, 0, 1, prec, 4, 0, 0))
+        for sched, kb, trav, tile in [(0, 4, 0, 0), (1, 8, 0, 1), (2, 4, 0, 2), (3, 4, 0, 1), (0, 4, 1, 0),
+                                      (1, 8, 1, 2), (3, 8, 1, 0)]:
+            out = torch.full_like(ref, -1.0)
+            scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, prec, kb, trav, tile))
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(out.cpu().numpy(), ref.cpu().numpy())
     assert scene.status() == 0
     scene.close()

@@ -38,7 +38,7 @@ def test_golden_scenes_bit_exact(pkg, O, cuda, fixtures, name):
 
 
 @pytest.mark.parametrize("case", ["analytic", "straddle", "comb", "ties", "ties_perm", "big_leaf", "empty",
-                                  "miss"])
+                                  "miss", "mixed_aniso"])
 def test_known_answer_scenes_bit_exact(pkg, O, cuda, case):
     if case == "analytic":
         tree, rec, cam = kat.analytic_single()
@@ -61,6 +61,9 @@ def test_known_answer_scenes_bit_exact(pkg, O, cuda, case):
     elif case == "empty":
         tree, rec, cam = kat.empty()
         W = H = 8
+    elif case == "mixed_aniso":
+        tree, rec, cam = kat.mixed_aniso()
+        W = H = 16
     else:
         tree, rec, cam = kat.miss()
         W = H = 8
