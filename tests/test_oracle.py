@@ -170,3 +170,16 @@ def test_fp32_vs_fp64_close(O, fixtures):
     r32, _, _, _ = O.render(S, cam, w, h)
     r64, _, _, _ = O.render(S, cam, w, h, precision="f64")
     assert np.sqrt(((r32 - r64) ** 2).mean()) < 1e-4
+
+
+def test_thin_gaussians_fp32_vs_fp64(O):
+    """Very thin Gaussians (scale ratio 2000) seen edge-on and face-on: the
+    FP32 transcription of the reference test stays within the fast forms'
+    accuracy bar of the FP64 twin, and both composite the same leaves."""
+    tree, rec, cam = kat.mixed_aniso()
+    S = oscene(O, tree, rec)
+    r32, a32, _, tr = O.render(S, cam, 16, 16, trace=True)
+    r64, a64, _, _ = O.render(S, cam, 16, 16, precision="f64")
+    assert np.sqrt(((r32 - r64) ** 2).mean()) < 1e-3
+    assert np.sqrt(((a32 - a64) ** 2).mean()) < 1e-3
+    assert tr["n_leaf"].max() == 2 and tr["n_blend"].max() > 0
