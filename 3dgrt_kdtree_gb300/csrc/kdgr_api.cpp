@@ -357,6 +357,7 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
 
 int kdgr_scene_destroy(kdgr_scene_t s) {
   if (!s) return KDGR_ERR_INVALID_ARG;
+  DeviceScope on(s->device);
   void* ps[] = {s->d_nodes,     s->d_offsets, s->d_test,      s->d_sh,          s->d_nodes_fast,
                 s->d_opacity,   s->d_sh_bf16,     s->d_leaf_pairs,  s->d_leaf_packed, s->d_pair_gid,
                 s->d_nodes_packed, s->d_leaf_aux, s->d_gid_plain, s->d_gid_flag, s->d_flag_pairs,
@@ -395,7 +396,9 @@ int kdgr_scene_status(kdgr_scene_t s, uint32_t* bits, int clear) {
     set_error("kdgr_scene_status: null argument");
     return KDGR_ERR_INVALID_ARG;
   }
-  cudaError_t e = cudaDeviceSynchronize();
+  DeviceScope on(s->device);
+  cudaError_t e = on.err;
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(bits, s->d_status, 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && clear) e = cudaMemset(s->d_status, 0, 4);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_status");
@@ -412,6 +415,8 @@ static int render_common(kdgr_scene_t s, const kdgr_camera* cam, int W, int H, f
     set_error(std::string(who) + ": scene was created without KDGR_FORM_EXACT");
     return KDGR_ERR_INVALID_ARG;
   }
+  DeviceScope on(s->device);
+  if (on.err != cudaSuccess) return cuda_fail(on.err, who);
   const cudaStream_t st = (cudaStream_t)stream;
   const CamInfo ci = make_caminfo(*cam, W, H);
   cudaEvent_t e0 = nullptr, e1 = nullptr;

@@ -85,6 +85,8 @@ int kdgr_render_batch(kdgr_scene_t s, const kdgr_view* views, int n_views, float
   uint32_t totals[3] = {0, 0, 0};
   rc = make_view_table(views, n_views, table, totals);
   if (rc != KDGR_OK) return rc;
+  DeviceScope on(s->device);
+  if (on.err != cudaSuccess) return cuda_fail(on.err, "kdgr_render_batch");
   const cudaStream_t st = (cudaStream_t)stream;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (ms_out) {
@@ -137,6 +139,8 @@ int kdgr_batch_create(kdgr_scene_t s, const kdgr_view* views, int n_views, float
   uint32_t totals[3] = {0, 0, 0};
   rc = make_view_table(views, n_views, table, totals);
   if (rc != KDGR_OK) return rc;
+  DeviceScope on(s->device);
+  if (on.err != cudaSuccess) return cuda_fail(on.err, "kdgr_batch_create");
   kdgr_batch_s* b = new kdgr_batch_s;
   b->scene = s;
   b->cfg = c;
@@ -171,13 +175,16 @@ int kdgr_batch_run(kdgr_batch_t b, void* stream) {
     set_error("kdgr_batch_run: invalid batch");
     return KDGR_ERR_INVALID_ARG;
   }
-  cudaError_t e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
+  DeviceScope on(b->scene->device);
+  cudaError_t e = on.err;
+  if (e == cudaSuccess) e = cudaGraphLaunch(b->exec, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_batch_run");
   return KDGR_OK;
 }
 
 int kdgr_batch_destroy(kdgr_batch_t b) {
   if (!b) return KDGR_ERR_INVALID_ARG;
+  DeviceScope on(b->scene->device);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   if (b->d_views) cudaFree(b->d_views);
@@ -201,6 +208,8 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
   uint32_t totals[3] = {0, 0, 0};
   rc = make_view_table(views, n_views, table, totals);
   if (rc != KDGR_OK) return rc;
+  DeviceScope on(s->device);
+  if (on.err != cudaSuccess) return cuda_fail(on.err, "kdgr_autotune");
   std::vector<kdgr_batch_config> cands;
   for (int minb : {0, 6, 8})
     for (int sched : {KDGR_SCHED_WARP_TILES, KDGR_SCHED_CTA_BLOCKS, KDGR_SCHED_SM_STRIPS, KDGR_SCHED_WARP_STRIPS})

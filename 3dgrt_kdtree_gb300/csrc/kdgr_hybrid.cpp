@@ -215,6 +215,8 @@ int kdgr_render_hybrid(kdgr_scene_t s, const kdgr_camera* cam, int W, int H, kdg
     set_error("kdgr_render_hybrid: scene was created without KDGR_FORM_EXACT");
     return KDGR_ERR_INVALID_ARG;
   }
+  DeviceScope on(s->device);
+  if (on.err != cudaSuccess) return cuda_fail(on.err, "kdgr_render_hybrid");
   const cudaStream_t st = (cudaStream_t)stream;
   const CamInfo ci = make_caminfo(*cam, W, H);
   HybridView m{sec->d_spheres, sec->d_tris, sec->d_tri_material, sec->n_spheres, sec->n_tris};

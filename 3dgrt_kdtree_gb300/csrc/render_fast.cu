@@ -40,6 +40,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cstdint>
 #include <cstring>
@@ -986,16 +987,20 @@ KernelFn pick_kernel(const kdgr_batch_config& c) {
   return c.precision ? pick_sched<true>(c) : pick_sched<false>(c);
 }
 
-int g_num_sms = 0;
+// SM count of the current device, cached per device.  Threads may race on
+// the first query of a device; they all store the same value.
+constexpr int kMaxSmCacheDevices = 64;
+std::atomic<int> g_num_sms[kMaxSmCacheDevices];
 
 int num_sms() {
-  if (g_num_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_num_sms <= 0) g_num_sms = 1;
-  }
-  return g_num_sms;
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+  const bool cacheable = dev >= 0 && dev < kMaxSmCacheDevices;
+  if (cacheable) n = g_num_sms[dev].load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  if (dev < 0 || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+  if (cacheable) g_num_sms[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 }  // namespace
@@ -1003,39 +1008,11 @@ int num_sms() {
 // Host: view table and total tile count for a list of views.
 int make_view_table(const kdgr_view* views, int n_views, std::vector<ViewDesc>& out, uint32_t totals[3]) {
   out.resize(n_views);
-  uint64_t wbase = 0, cbase = 0;
-  for (int v = 0; v < n_views; ++v) {
-    const kdgr_view& kv = views[v];
-    if (kv.width <= 0 || kv.height <= 0) {
-      set_error("view " + std::to_string(v) + " has an empty image");
-      return KDGR_ERR_INVALID_ARG;
-    }
-    ViewDesc& d = out[v];
-    d.cam = make_caminfo(kv.cam, kv.width, kv.height);
-    d.W = kv.width;
-    d.H = kv.height;
-    d.wt_x = (uint32_t)((kv.width + kTileW - 1) / kTileW);
-    d.wt_base = (uint32_t)wbase;
-    d.cb_x = (uint32_t)((kv.width + kBlockW - 1) / kBlockW);
-    d.cb_base = (uint32_t)cbase;
-    d.out_off = kv.out_offset;
-    d.scene = 0;
-    d.pad = 0;
-    wbase += (uint64_t)d.wt_x * (uint64_t)((kv.height + kTileH - 1) / kTileH);
-    cbase += (uint64_t)d.cb_x * (uint64_t)((kv.height + kBlockH - 1) / kBlockH);
-    if (wbase > 0xF0000000ull) {
-      set_error("batch too large: more than 2^32 tiles");
-      return KDGR_ERR_LIMIT;
-    }
-  }
-  totals[0] = (uint32_t)wbase;
-  totals[1] = (uint32_t)cbase;
-  totals[2] = 0;
-  return KDGR_OK;
+  return fill_view_table(views, n_views, out.data(), totals);
 }
 
-// As make_view_table, into a caller-provided array of n_views entries (no
-// allocation).
+// The view table of n_views views into a caller-provided array (no
+// allocation); make_view_table and the allocation-free entry point share it.
 int fill_view_table(const kdgr_view* views, int n_views, ViewDesc* out, uint32_t totals[3]) {
   uint64_t wbase = 0, cbase = 0;
   for (int v = 0; v < n_views; ++v) {

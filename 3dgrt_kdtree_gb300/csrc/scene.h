@@ -55,6 +55,24 @@ struct kdgr_scene_s {
 };
 
 namespace kdgr {
+// Makes `device` current for the enclosing scope and restores the caller's
+// device afterwards: every call on a scene runs on the device the scene was
+// created on, whatever device the calling thread has selected.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceScope(int device) {
+    err = cudaGetDevice(&prev);
+    if (err == cudaSuccess && prev != device) err = cudaSetDevice(device);
+    else prev = -1;  // nothing to restore
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
 // Allocation helper that records bytes and frees everything on failure.
 struct DevAlloc {
   std::vector<void*> ptrs;

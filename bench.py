@@ -4,7 +4,10 @@
 
 A step renders one batch of views of a resident scene.  Configurations:
 
-  scale     (default) 1M-Gaussian cluster+shell scene, one 1920x1080 view
+  scale     (default) 1M-Gaussian cluster+shell scene, one 1920x1080 view;
+            the line also carries two short legs on the same GPU: the
+            64-view batch of the same scene (`legs.batching`) and the
+            serving loop at one request rate (`legs.serving`)
   small     100k Gaussians uniform in the unit cube, one 256x256 view
   batching  the 1M scene, 64 views on spheres of radius 2-4 (16 each at
             256x256, 640x480, 1280x720, 1920x1080) in one persistent launch
@@ -23,25 +26,39 @@ the plain kernel against the oracle-matching FP32 oracle (expected 0).
 
 `value` is the batched (persistent, CUDA-graph) form with the scene resident
 in HBM, timed with CUDA events per step with an L2 flush (a 512 MB write)
-between steps.  `e2e` is the same metric through the C ABI with host-side
-cameras and the frame read back into pinned host memory every step.
+between steps.  `e2e` is the same metric through the C ABI
+(kdgr_render_batch) timed on the host clock: from the call (cameras in host
+memory) to the frame being readable in pinned host memory, with no other
+work on the GPU (the L2 flush runs and completes before the clock starts).
+`roofline` is the issue-rate bound the kernel has (it is not bandwidth
+bound: its working set stays in L2): warp instructions per launch (from the
+ncu capture of the same launch, profiles/instructions.txt) over the
+measured kernel time, against 4 warp instructions per SM per cycle at the
+SM clock sampled during the timed region.  `roofline.memory` keeps the
+algorithmic bytes (L1/L2 demand) and the DRAM bytes of that capture.
+
 `--impl reference` times the reference algorithm's CPU implementation (the
 oracle transcription of cudaRenderer.cu, all host threads) on a strided ray
-sample of the same workload.  Multi-GPU: scene replicas, no collective in
-the data path (views are independent), weak scaling.
+sample of the same workload.  Its process loads only the oracle: the scene
+and its kd-tree are prepared by an untimed child process (seeded generation
+and the host kd-tree builder, whose trees are byte-identical to the
+reference builder's) and read back from files (the tree through the
+oracle's .kdt reader).  Multi-GPU: scene replicas, no collective in the data
+path (views are independent), weak scaling.
 """
 from __future__ import annotations
 
 import argparse
-import ctypes
 import importlib
 import json
 import os
+import shutil
 import statistics
 import subprocess
 import sys
 import tempfile
 import time
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -52,15 +69,20 @@ METRIC = "Mrays/s at 1080p/1M Gaussians"
 UNIT = "Mrays/s"
 PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+PKG = "3dgrt_kdtree_gb300"
 
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def _scenes():
+    """The seeded scene generator (numpy only)."""
+    return importlib.import_module(PKG + ".scenes")
+
+
 # ------------------------------------------------------------------ workload
-def make_workload(pkg, name: str):
-    sc = pkg.scenes
+def make_workload(sc, name: str):
     if name == "small":
         rec = sc.uniform_cube(100_000, seed=0)
         cams = [(sc.front_camera(256, 256), 256, 256)]
@@ -75,7 +97,7 @@ def make_workload(pkg, name: str):
         desc = {"workload": "cluster+shell, 300k Gaussians, 1 view 1280x720", "gaussians": 300_000}
     elif name == "batching":
         rec = sc.cluster_shell(1_000_000, seed=1)
-        cams = sc.sphere_cameras(64, seed=11)
+        cams = batching_cameras(sc)
         desc = {"workload": "cluster+shell, 1M Gaussians, 64 mixed-resolution views", "gaussians": 1_000_000}
     elif name == "precision":
         rec = sc.cluster_shell(3_000_000, seed=2, n_clusters=256)
@@ -87,6 +109,16 @@ def make_workload(pkg, name: str):
     desc["rays_per_step"] = int(sum(w * h for _, w, h in cams))
     desc["views"] = len(cams)
     return rec, cams, desc
+
+
+def batching_cameras(sc):
+    """64 views on spheres of radius 2-4, 16 each at the four resolutions."""
+    return sc.sphere_cameras(64, seed=11)
+
+
+def common_config(desc: dict, world: int) -> dict:
+    """The `config` object both arms print (same workload, same keys)."""
+    return {**desc, "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -122,12 +154,12 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sm)}
 
 
-# ------------------------------------------------------------------ helpers
-def hbm_peak():
+# ------------------------------------------------------------------ roofline
+def peaks() -> dict:
     try:
-        return float(json.load(open(PEAKS))["hbm_gbs"]), "measured"
-    except Exception:
-        return FALLBACK_HBM_GBS, "fallback"
+        return json.load(open(PEAKS))
+    except (OSError, ValueError):
+        return {}
 
 
 def algorithmic_bytes(tr, b_test: int, b_blend: int, b_out: int) -> float:
@@ -139,28 +171,92 @@ def algorithmic_bytes(tr, b_test: int, b_blend: int, b_out: int) -> float:
                  + b_out * n)
 
 
-def load_traffic():
-    """profiles/traffic.txt: `config:form bytes` lines (# comments)."""
-    out = {}
+def load_capture(key: str):
+    """profiles/instructions.txt: `config:form kernel warp_instructions
+    dram_bytes duration_ns` per line (# comments), from one ncu capture of
+    one launch of the batched kernel."""
     try:
-        for line in open(os.path.join(REPO, "profiles", "traffic.txt")):
+        for line in open(os.path.join(REPO, "profiles", "instructions.txt")):
             f = line.split("#", 1)[0].split()
-            if len(f) == 2:
-                out[f[0]] = int(f[1])
+            if len(f) == 5 and f[0] == key:
+                return {"kernel": f[1], "warp_instructions": int(f[2]), "dram_bytes": int(f[3]),
+                        "duration_ns": int(f[4])}
     except (OSError, ValueError):
-        return {}
+        pass
+    return None
+
+
+def roofline(key: str, ms_step: float, clk: dict, sms: int, alg_bytes: float, rays: int) -> dict:
+    """Issue-rate bound of the batched kernel, plus its memory figures."""
+    pk = peaks()
+    hbm = float(pk.get("hbm_gbs", FALLBACK_HBM_GBS))
+    mhz = clk.get("sm_mhz") or float(pk.get("sm_max_mhz", 2070.0))
+    mhz_src = "median SM clock sampled in the timed region" if clk.get("sm_mhz") else \
+        "SM clock not sampled in the timed region: maximum SM clock of MEASURED_PEAKS.json"
+    cap = load_capture(key)
+    peak = sms * 4 * mhz * 1e6 / 1e9  # G warp instructions / s
+    out = {"bound": "issue", "unit": "G warp-inst/s", "peak": round(peak, 2),
+           "peak_source": f"{sms} SMs x 4 schedulers x 1 warp instruction per cycle x {mhz:.0f} MHz ({mhz_src})"}
+    if cap:
+        ach = cap["warp_instructions"] / (ms_step * 1e-3) / 1e9
+        prof_frac = cap["warp_instructions"] / (sms * 4 * 2070e6 * cap["duration_ns"] * 1e-9)
+        out.update({"achieved": round(ach, 2), "frac": round(ach / peak, 4),
+                    "warp_instructions_per_launch": cap["warp_instructions"],
+                    "warp_instructions_per_ray": round(cap["warp_instructions"] / rays, 1),
+                    "instructions_from": f"ncu smsp__inst_executed.sum of one launch of {cap['kernel']} "
+                                         f"(profiles/instructions.txt); frac of that capture at its own "
+                                         f"duration: {prof_frac:.4f}",
+                    "traffic": cap["dram_bytes"]})
+    else:
+        out.update({"achieved": None, "frac": None, "traffic": None,
+                    "instructions_from": f"no capture for {key} in profiles/instructions.txt"})
+    dram = cap["dram_bytes"] if cap else None
+    out["memory"] = {
+        "algorithmic_bytes_per_step": alg_bytes, "bytes_per_ray": round(alg_bytes / rays, 1),
+        "algorithmic_gbs": round(alg_bytes / (ms_step * 1e-3) / 1e9, 1),
+        "note": "algorithmic bytes are L1/L2 demand: the frame's working set stays in the 126 MB L2",
+        "dram_bytes_per_launch": dram,
+        "dram_gbs": round(dram / (ms_step * 1e-3) / 1e9, 2) if dram else None,
+        "dram_frac_of_hbm": round(dram / (ms_step * 1e-3) / 1e9 / hbm, 5) if dram else None,
+        "hbm_peak_gbs": hbm, "hbm_peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk
+        else "fallback 6.8 TB/s"}
     return out
 
 
 # ------------------------------------------------------------------ our arm
+def timed_loop(step_fn, k, flush, stream, dev):
+    import torch
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+    for i in range(k):
+        flush.zero_()
+        evs[i][0].record(stream)
+        step_fn()
+        evs[i][1].record(stream)
+    torch.cuda.synchronize(dev)
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def wall_loop(step_fn, k, flush, dev):
+    """Host-clock time of each step, the L2 flush completed before the clock starts."""
+    import torch
+    out = []
+    for _ in range(k):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        step_fn()
+        out.append(1e3 * (time.perf_counter() - t0))
+    return out
+
+
 def run_ours(args, rank: int, world: int):
     import torch
-    pkg = importlib.import_module("3dgrt_kdtree_gb300")
+    pkg = importlib.import_module(PKG)
     F = pkg.renderer
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     F.init(dev.index)
-    rec, cams, desc = make_workload(pkg, args.config)
+    rec, cams, desc = make_workload(pkg.scenes, args.config)
     t0 = time.time()
     tree = pkg.kdtree.build(rec, device="cuda")  # the device builder: same tree as the host builder
     build_s = time.time() - t0
@@ -182,7 +278,6 @@ def run_ours(args, rank: int, world: int):
         log("[bench] autotuner variants:\n" + report.strip())
         log(f"[bench] autotuner picked {cfg.as_dict()}")
     batch = F.Batch(scene, views, len(cams), rgb, None, None, cfg)
-    flush = torch.empty((16 if args.profile else 512 * 1024 * 1024) // 4, dtype=torch.float32, device=dev)
     if args.profile:
         for _ in range(args.warmup + args.steps):
             for (cam, w, h), off in zip(cams, offs):
@@ -193,17 +288,8 @@ def run_ours(args, rank: int, world: int):
         assert scene.status() == 0
         print(json.dumps({"profile_run": args.config, "launches": args.warmup + args.steps}), flush=True)
         raise SystemExit(0)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
-
-    def timed_loop(step_fn, k):
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
-        for i in range(k):
-            flush.zero_()
-            evs[i][0].record(stream)
-            step_fn()
-            evs[i][1].record(stream)
-        torch.cuda.synchronize(dev)
-        return [a.elapsed_time(b) for a, b in evs]
 
     for _ in range(args.warmup):
         batch.run()
@@ -213,31 +299,35 @@ def run_ours(args, rank: int, world: int):
     torch.cuda.synchronize(dev)
     clocks = ClockSampler(dev.index)
     wall0 = time.time()
-    ms = timed_loop(batch.run, args.steps)
+    ms = timed_loop(batch.run, args.steps, flush, stream, dev)
     wall = time.time() - wall0
     clk = clocks.stop()
     if world > 1:
         torch.distributed.barrier()
     assert scene.status() == 0, "kernel raised an error status"
-    R = importlib.import_module("3dgrt_kdtree_gb300.replicas")
+    R = importlib.import_module(PKG + ".replicas")
     ms_step = R.max_over_ranks(sum(ms) / len(ms), dev)
     value = R.job_throughput(rays, world, ms_step) / 1e6
 
-    # e2e: cameras from the host each step, frame read back into pinned memory
+    # e2e: the public C ABI call with host-side cameras, the frame read back
+    # into pinned host memory, timed on the host clock
     host = torch.empty(total_px * 3, dtype=torch.float32, pin_memory=True)
 
     def e2e_step():
         scene.render_batch(views, len(cams), rgb, cfg=cfg)
         host.copy_(rgb, non_blocking=True)
+        stream.synchronize()
 
     for _ in range(args.warmup):
         e2e_step()
-    ms_e2e = timed_loop(e2e_step, args.steps)
-    e2e_step_ms = R.max_over_ranks(sum(ms_e2e) / len(ms_e2e), dev)
+    ms_e2e = wall_loop(e2e_step, args.steps, flush, dev)
+    e2e_step_ms = R.max_over_ranks(statistics.median(ms_e2e), dev)
     view_bytes = 96 * len(cams)  # ViewDesc table (96 B per view) copied host->device by kdgr_render_batch
-    e2e = {"value": R.job_throughput(rays, world, e2e_step_ms) / 1e6, "unit": UNIT, "h2d_bytes_per_step": view_bytes,
-           "d2h_bytes_per_step": int(host.numel() * 4), "ms_per_step": e2e_step_ms,
-           "path": "kdgr_render_batch (C ABI) + D2H of the RGB frame"}
+    e2e = {"value": R.job_throughput(rays, world, e2e_step_ms) / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": view_bytes, "d2h_bytes_per_step": int(host.numel() * 4),
+           "ms_per_step": e2e_step_ms, "ms_per_step_mean": statistics.mean(ms_e2e),
+           "clock": "host perf_counter, median over steps: call -> frame readable in pinned host memory",
+           "path": "kdgr_render_batch (C ABI) + D2H of the RGB frame + stream sync"}
 
     # plain drop-in (oracle-matching) kernel on the same views, one launch per view
     def plain_step():
@@ -247,27 +337,16 @@ def run_ours(args, rank: int, world: int):
     batched_host = host.numpy().copy()  # the last batched frame (e2e loop)
     for _ in range(max(1, args.warmup // 2)):
         plain_step()
-    pm = timed_loop(plain_step, max(2, args.steps // 2))
+    pm = timed_loop(plain_step, max(2, args.steps // 2), flush, stream, dev)
     plain_ms = sum(pm) / len(pm)
     torch.cuda.synchronize(dev)
     plain_host = rgb.cpu().numpy().copy()
 
     # counters of the oracle-matching kernel -> algorithmic bytes per step
-    tr_all = []
-    for (cam, w, h), off in zip(cams, offs):
-        if not (forms & F.FORM_EXACT):
-            break
-        tr = torch.zeros(w * h * np.dtype(pkg.capi.TRACE_DTYPE).itemsize, dtype=torch.uint8, device=dev)
-        tmp = torch.zeros(w * h * 3, device=dev)
-        scene.render_trace(cam, w, h, tmp, None, None, tr)
-        torch.cuda.synchronize(dev)
-        tr_all.append(np.frombuffer(tr.cpu().numpy().tobytes(), dtype=np.dtype(pkg.capi.TRACE_DTYPE)))
-    tr_cat = np.concatenate(tr_all)
+    tr_cat = trace_counters(pkg, scene, cams, dev)
     b_test, b_blend = (32, 96 + 2) if precision else (48, 192 + 4)
     alg_bytes = algorithmic_bytes(tr_cat, b_test, b_blend, 12)
-    peak, peak_kind = hbm_peak()
-    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
-    traffic = load_traffic().get(f"{args.config}:{'packed' if precision else 'fp32'}")
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     counters = {k: float(tr_cat[k].mean()) for k in ("n_inner", "n_leaf", "n_cand", "n_hit", "n_blend",
                                                      "n_restart")}
     out = {
@@ -275,14 +354,11 @@ def run_ours(args, rank: int, world: int):
         "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16/fp16 storage, fp32 arithmetic" if precision else "f32", "data": "synthetic",
-        "config": {**desc, "form": "batched persistent kernel, CUDA graph", "autotuned": cfg.as_dict(),
-                   "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"},
+        "config": common_config(desc, world),
+        "form": "batched persistent kernel, CUDA graph", "autotuned": cfg.as_dict(),
         "e2e": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in e2e.items()},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                     else "fallback 6.8 TB/s",
-                     "algorithmic_bytes_per_step": alg_bytes, "bytes_per_ray": round(alg_bytes / rays, 1)},
+        "roofline": roofline(f"{args.config}:{'packed' if precision else 'fp32'}", ms_step, clk, sms, alg_bytes,
+                             rays),
         "gpu_launches": args.steps,
         "clocks": clk,
         "forms": {"plain_ms_per_step": plain_ms,
@@ -293,11 +369,71 @@ def run_ours(args, rank: int, world: int):
                  "build_s": round(build_s, 2)},
         "wall_s_timed": round(wall, 3),
     }
-    if rank == 0 and not args.no_cpu_baseline:
+    check = rank == 0 and not args.no_cpu_baseline
+    if check:
         out["cpu_baseline"] = cpu_baseline(tree, rec, cams, args.cpu_seconds)
         out["accuracy"] = accuracy(tree, rec, cams, offs, batched_host, plain_host)
+    if args.config == "scale" and not args.no_legs and rank == 0:
+        out["legs"] = {"batching": leg_batching(pkg, scene, tree, rec, dev, flush, stream, args, check)}
     batch.close()
     scene.close()
+    if args.config == "scale" and not args.no_legs and rank == 0:
+        del flush
+        torch.cuda.empty_cache()
+        srv = run_serving_rates(pkg, [args.leg_rate], args.leg_seconds)
+        out["legs"]["serving"] = {"rate_req_s": args.leg_rate, "seconds": args.leg_seconds, **srv["results"],
+                                  "setup": srv["setup"]}
+    return out
+
+
+def trace_counters(pkg, scene, cams, dev):
+    import torch
+    tr_all = []
+    dt = np.dtype(pkg.capi.TRACE_DTYPE)
+    for cam, w, h in cams:
+        tr = torch.zeros(w * h * dt.itemsize, dtype=torch.uint8, device=dev)
+        tmp = torch.zeros(w * h * 3, device=dev)
+        scene.render_trace(cam, w, h, tmp, None, None, tr)
+        torch.cuda.synchronize(dev)
+        tr_all.append(np.frombuffer(tr.cpu().numpy().tobytes(), dtype=dt))
+    return np.concatenate(tr_all)
+
+
+def leg_batching(pkg, scene, tree, rec, dev, flush, stream, args, check: bool):
+    """The 64-view batch of the same 1M scene (one persistent launch, CUDA
+    graph, autotuned) against the plain kernel, one launch per view."""
+    import torch
+    F = pkg.renderer
+    cams = batching_cameras(pkg.scenes)
+    views, total, offs = F.make_views(cams)
+    rays = int(sum(w * h for _, w, h in cams))
+    rgb = torch.zeros(total * 3, device=dev)
+    cfg, _ = scene.autotune(views, len(cams), rgb, precision=0)
+    batch = F.Batch(scene, views, len(cams), rgb, None, None, cfg)
+    for _ in range(2):
+        batch.run()
+    k = max(3, args.steps // 5)
+    ms = statistics.mean(timed_loop(batch.run, k, flush, stream, dev))
+    torch.cuda.synchronize(dev)
+    batched_host = rgb.cpu().numpy().copy()
+    batch.close()
+
+    def plain_step():
+        for (cam, w, h), off in zip(cams, offs):
+            scene.render(cam, w, h, rgb[3 * off:3 * (off + w * h)])
+
+    plain_step()
+    pms = statistics.mean(timed_loop(plain_step, 2, flush, stream, dev))
+    torch.cuda.synchronize(dev)
+    assert scene.status() == 0
+    out = {"workload": "cluster+shell, 1M Gaussians, 64 views (16 each at 256x256, 640x480, 1280x720, "
+                       "1920x1080) in one persistent launch", "rays_per_step": rays, "steps": k,
+           "ms_per_step": round(ms, 3), "mrays_s": round(rays / (ms * 1e-3) / 1e6, 2),
+           "plain_ms_per_step": round(pms, 3), "plain_mrays_s": round(rays / (pms * 1e-3) / 1e6, 2),
+           "batched_over_plain": round(pms / ms, 3), "autotuned": cfg.as_dict()}
+    if check:
+        plain_host = rgb.cpu().numpy().copy()
+        out["accuracy"] = accuracy(tree, rec, cams, offs, batched_host, plain_host, n_target=20000)
     return out
 
 
@@ -305,8 +441,7 @@ def run_ours(args, rank: int, world: int):
 def poisson_requests(rate: float, seconds: float, n_scenes: int, seed: int):
     """[(arrival_s, scene, [(Camera, W, H)])]: Poisson arrivals, 1-16 views per
     request, each view's resolution uniform over the four, scene uniform."""
-    import importlib as _il
-    sc = _il.import_module("3dgrt_kdtree_gb300.scenes")
+    sc = _scenes()
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
     while True:
@@ -323,14 +458,13 @@ def poisson_requests(rate: float, seconds: float, n_scenes: int, seed: int):
         out.append((t, int(rng.integers(0, n_scenes)), cams))
 
 
-def run_serving(args):
+def run_serving_rates(pkg, rates, seconds):
     """Four resident scenes (0.5M/1M/2M/3M cluster+shell, seeds 1-4) under a
     60 GB budget; Poisson request streams at each rate, served by the
     continuous-batching server, and by the plain per-request path (one
     request at a time, one plain-kernel launch per view) for comparison."""
     import threading
     import torch
-    pkg = importlib.import_module("3dgrt_kdtree_gb300")
     F = pkg.renderer
     F.init(0)
     sizes = [500_000, 1_000_000, 2_000_000, 3_000_000]
@@ -342,12 +476,12 @@ def run_serving(args):
         tree = pkg.kdtree.build(rec, device="cuda")
         slots.append(srv.add_scene(tree, rec))
         plain_scenes.append(F.Scene(tree, rec, forms=F.FORM_EXACT))
-    log(f"[bench] serving: 4 scenes built and resident in {time.time() - t0:.1f}s, "
-        f"{srv.stats()['resident_bytes'] / 1e9:.1f} GB of the 60 GB budget")
-    rates = [float(r) for r in args.rates.split(",")]
+    setup = {"seconds": round(time.time() - t0, 1), "resident_gb": round(srv.stats()["resident_bytes"] / 1e9, 2),
+             "budget_gb": 60.0 * (1 << 30) / 1e9}
+    log(f"[bench] serving: 4 scenes built and resident in {setup['seconds']}s, {setup['resident_gb']} GB")
     results = {}
     for rate in rates:
-        reqs = poisson_requests(rate, args.serve_seconds, len(sizes), seed=int(rate))
+        reqs = poisson_requests(rate, seconds, len(sizes), seed=int(rate))
         rays = sum(w * h for _, _, cams in reqs for _, w, h in cams)
         # served
         srv.reset_stats()
@@ -410,9 +544,21 @@ def run_serving(args):
             "plain": {"p50_ms": round(pct(lat, 0.5), 2), "p99_ms": round(pct(lat, 0.99), 2),
                       "mrays_per_s": round(rays / plain_wall / 1e6, 1)},
         }
-        log(f"[bench] rate {rate}: {results[str(int(rate))]}")
-    key = "50" if "50" in results else list(results)[0]
+        r = results[str(int(rate))]
+        r["p99_plain_over_served"] = round(r["plain"]["p99_ms"] / max(r["served"]["p99_ms"], 1e-9), 2)
+        log(f"[bench] rate {rate}: {r}")
     srv.close()
+    for s in plain_scenes:
+        s.close()
+    return {"results": results, "setup": setup}
+
+
+def run_serving(args):
+    pkg = importlib.import_module(PKG)
+    rates = [float(r) for r in args.rates.split(",")]
+    res = run_serving_rates(pkg, rates, args.serve_seconds)
+    results = res["results"]
+    key = "50" if "50" in results else list(results)[0]
     return {
         "metric": f"served p99 latency at {key} req/s", "value": results[key]["served"]["p99_ms"], "unit": "ms",
         "n_gpus": 1, "steps": len(rates), "warmup": 0, "higher_is_better": False, "scaling": "weak",
@@ -420,17 +566,25 @@ def run_serving(args):
         "config": {"workload": "4 resident cluster+shell scenes (0.5M/1M/2M/3M), Poisson requests of 1-16 "
                                "views at 256x256/640x480/1280x720/1920x1080, 60 GB budget",
                    "form": "continuous-batching server, 3 lanes", "seconds_per_rate": args.serve_seconds},
-        "serving": results,
+        "serving": results, "setup": res["setup"],
     }
 
 
 # ------------------------------------------------------------------ CPU arm
-def cpu_sample(tree, rec, cams, seconds: float, threads: int = 0, precision: str = "f32"):
-    """Render a strided ray sample of every view with the oracle (CPU), sized
-    to about `seconds` of work.  Returns (Mrays/s, rays, stride, threads)."""
+def _oracle():
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O
-    S = O.OracleScene(tree.nodes, tree.offsets, tree.aabb, O.invert_scales(rec))
+    return importlib.import_module("oracle")
+
+
+def oracle_scene(tree, rec):
+    O = _oracle()
+    return O.OracleScene(tree.nodes, tree.offsets, tree.aabb, O.invert_scales(rec))
+
+
+def cpu_sample(S, cams, seconds: float, threads: int = 0, precision: str = "f32"):
+    """Render a strided ray sample of every view with the oracle (CPU), sized
+    to about `seconds` of work.  Returns (Mrays/s, rays, stride, threads, s)."""
+    O = _oracle()
     nthr = threads or os.cpu_count() or 1
 
     def run(stride):
@@ -455,9 +609,8 @@ def accuracy(tree, rec, cams, offs, batched, plain, n_target: int = 40000):
     """Max and RMS RGB error of the batched frame against the FP64 oracle,
     and of the plain kernel against the FP64 and the oracle-matching FP32
     oracle, on a strided ray sample of every view."""
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O
-    S = O.OracleScene(tree.nodes, tree.offsets, tree.aabb, O.invert_scales(rec))
+    O = _oracle()
+    S = oracle_scene(tree, rec)
     total = sum(w * h for _, w, h in cams)
     stride = max(1, total // n_target)
     eb, ep, ep32 = [], [], []
@@ -477,12 +630,109 @@ def accuracy(tree, rec, cams, offs, batched, plain, n_target: int = 40000):
             "plain_vs_fp32_oracle_max_abs": float(np.abs(ep32).max())}
 
 
+def cpu_baseline(tree, rec, cams, seconds):
+    S = oracle_scene(tree, rec)
+    mr, n, stride, nthr, dt = cpu_sample(S, cams, seconds)
+    mr1, n1, _, _, dt1 = cpu_sample(S, cams, max(1.0, seconds / 4), threads=1)
+    mr64, n64, _, _, dt64 = cpu_sample(S, cams, max(1.0, seconds / 4), precision="f64")
+    return {"value": round(mr, 4), "unit": UNIT, "cores": nthr, "kind": "port",
+            "sample": f"every {stride}th ray of each view ({n} rays, {dt:.1f}s), oracle FP32 transcription "
+                      f"of cudaRenderer.cu with OpenMP over rays",
+            "single_thread_value": round(mr1, 4), "single_thread_sample": f"{n1} rays, {dt1:.1f}s",
+            "fp64_value": round(mr64, 4), "fp64_sample": f"{n64} rays, {dt64:.1f}s, {nthr} threads",
+            "cpu_model": cpu_model()}
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def prepare_reference_inputs(config: str, out_dir: str) -> None:
+    """Untimed input preparation of the reference arm, run as its own process:
+    the seeded scene and its kd-tree (host builder, trees byte-identical to
+    the reference builder's) written as files: scene.npy (activated 64-float
+    records), tree.kdt (the reference's binary format) and meta.json
+    (cameras, workload description, build time)."""
+    pkg = importlib.import_module(PKG)
+    rec, cams, desc = make_workload(pkg.scenes, config)
+    t0 = time.time()
+    tree = pkg.kdtree.build(rec)
+    build_s = time.time() - t0
+    np.save(os.path.join(out_dir, "scene.npy"), rec)
+    pkg.kdtree.write_kdt(tree, os.path.join(out_dir, "tree.kdt"))
+    meta = {"desc": desc, "build_s": build_s,
+            "cams": [{"cam": {"pos": list(c.pos), "uaxis": list(c.uaxis), "vaxis": list(c.vaxis),
+                              "naxis": list(c.naxis), "fovy": c.fovy, "aspect": c.aspect, "near_c": c.near_c},
+                      "w": w, "h": h} for c, w, h in cams]}
+    json.dump(meta, open(os.path.join(out_dir, "meta.json"), "w"))
+
+
+def run_reference(args):
+    """The reference's render algorithm on the host cores: the oracle
+    transcription of cudaRenderer.cu, all host threads, on a strided ray
+    sample per step.  This process loads the oracle only."""
+    O = _oracle()
+    work = tempfile.mkdtemp(prefix="kdgr_ref_")
+    try:
+        t0 = time.time()
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--prepare-reference", work, "--config",
+                        args.config], check=True, stdout=subprocess.DEVNULL)
+        prep_s = time.time() - t0
+        meta = json.load(open(os.path.join(work, "meta.json")))
+        rec = np.load(os.path.join(work, "scene.npy"))
+        nodes, offsets, aabb = O.read_kdt(os.path.join(work, "tree.kdt"))
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    desc = meta["desc"]
+    cams = [(SimpleNamespace(**c["cam"]), c["w"], c["h"]) for c in meta["cams"]]
+    S = O.OracleScene(nodes, offsets, aabb, O.invert_scales(rec))
+    per_step = max(2.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    res = []
+    for i in range(args.warmup + args.steps):
+        mr, n, stride, nthr, dt = cpu_sample(S, cams, per_step)
+        if i >= args.warmup:
+            res.append((mr, n, stride, dt))
+    value = statistics.mean(r[0] for r in res)
+    return {
+        "metric": METRIC if args.config == "scale" else f"Mrays/s ({args.config})", "impl": "reference",
+        "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * statistics.mean(r[3] for r in res), 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": common_config(desc, args.gpus),
+        "form": "CPU transcription of the reference render kernel (oracle, OpenMP over rays)",
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nthr, "kind": "port",
+                         "sample": f"every {res[-1][2]}th ray per view, {res[-1][1]} rays per step",
+                         "cpu_model": cpu_model()},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "inputs": {"prepared_by": "untimed child process: seeded scene generation and the host kd-tree builder "
+                                  "(trees byte-identical to the reference builder's, tests/test_kdtree.py); "
+                                  "read here from scene.npy and tree.kdt through the oracle's .kdt reader",
+                   "prep_s": round(prep_s, 1), "host_build_s": round(meta["build_s"], 2),
+                   "reference_builder": "not run here: it builds only from the reference's own sources, which "
+                                        "the GPU host does not have"},
+    }
+
+
 def run_build(args):
     """Tree build time on the bench scene: device builder against the host
     builder (all host cores), trees compared word for word."""
     pkg = importlib.import_module("3dgrt_kdtree_gb300")
     pkg.renderer.init(0)
-    rec, _, desc = make_workload(pkg, "scale")
+    rec, _, desc = make_workload(pkg.scenes, "scale")
     pkg.kdtree.build(pkg.scenes.uniform_cube(20_000, seed=5), device="cuda")  # context and pools warm
     times = []
     for _ in range(max(1, args.steps)):
@@ -513,7 +763,7 @@ def run_hybrid(args):
     F = pkg.renderer
     dev = torch.device("cuda", 0)
     F.init(0)
-    rec, cams, desc = make_workload(pkg, "scale")
+    rec, cams, desc = make_workload(pkg.scenes, "scale")
     tree = pkg.kdtree.build(rec, device="cuda")
     scene = F.Scene(tree, rec, forms=F.FORM_EXACT)
     quad = np.array([[-1.6, -1.6, -1.7, 1.6, -1.6, -1.7, 1.6, 1.6, -1.7],
@@ -556,9 +806,8 @@ def run_hybrid(args):
            "plain_ms_per_step": round(plain_ms, 4), "hybrid_over_plain_time": round(ms / plain_ms, 3),
            "clocks": clk, "gpu_launches": args.steps}
     if not args.no_cpu_baseline:
-        sys.path.insert(0, os.path.join(REPO, "oracle"))
-        import oracle as O
-        S = O.OracleScene(tree.nodes, tree.offsets, tree.aabb, O.invert_scales(rec))
+        O = _oracle()
+        S = oracle_scene(tree, rec)
         pix = np.arange(0, w * h, 211, dtype=np.uint32)
         sph = [(tuple(x.center), x.radius, x.material.material, x.material.reflectivity, x.material.ior,
                 tuple(x.material.color)) for x in F.demo_spheres()]
@@ -573,60 +822,6 @@ def run_hybrid(args):
     return out
 
 
-def cpu_baseline(tree, rec, cams, seconds):
-    mr, n, stride, nthr, dt = cpu_sample(tree, rec, cams, seconds)
-    mr1, n1, _, _, dt1 = cpu_sample(tree, rec, cams, max(1.0, seconds / 4), threads=1)
-    mr64, n64, _, _, dt64 = cpu_sample(tree, rec, cams, max(1.0, seconds / 4), precision="f64")
-    return {"value": round(mr, 4), "unit": UNIT, "cores": nthr, "kind": "port",
-            "sample": f"every {stride}th ray of each view ({n} rays, {dt:.1f}s), oracle FP32 transcription "
-                      f"of cudaRenderer.cu with OpenMP over rays",
-            "single_thread_value": round(mr1, 4), "single_thread_sample": f"{n1} rays, {dt1:.1f}s",
-            "fp64_value": round(mr64, 4), "fp64_sample": f"{n64} rays, {dt64:.1f}s, {nthr} threads",
-            "cpu_model": cpu_model()}
-
-
-def cpu_model() -> str:
-    try:
-        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
-        for line in out.splitlines():
-            if line.startswith("Model name:"):
-                return line.split(":", 1)[1].strip()
-    except (OSError, subprocess.SubprocessError):
-        pass
-    try:
-        for line in open("/proc/cpuinfo"):
-            if line.lower().startswith(("model name", "cpu part")):
-                return line.split(":", 1)[1].strip()
-    except OSError:
-        pass
-    import platform
-    return platform.machine()
-
-
-def run_reference(args):
-    pkg = importlib.import_module("3dgrt_kdtree_gb300")
-    rec, cams, desc = make_workload(pkg, args.config)
-    tree = pkg.kdtree.build(rec)
-    per_step = max(2.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
-    res = []
-    for i in range(args.warmup + args.steps):
-        mr, n, stride, nthr, dt = cpu_sample(tree, rec, cams, per_step)
-        if i >= args.warmup:
-            res.append((mr, n, stride, dt))
-    value = statistics.mean(r[0] for r in res)
-    out = {
-        "metric": METRIC if args.config == "scale" else f"Mrays/s ({args.config})", "impl": "reference",
-        "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1e3 * statistics.mean(r[3] for r in res), 2), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {**desc, "form": "CPU transcription of the reference render kernel (oracle, OpenMP)"},
-        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": nthr, "kind": "port",
-                         "sample": f"every {res[-1][2]}th ray per view, {res[-1][1]} rays per step"},
-        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    return out
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -636,12 +831,19 @@ def main():
                     choices=["scale", "small", "mid", "batching", "precision", "serving", "build", "hybrid"])
     ap.add_argument("--rates", default="50,100,200,400", help="serving: Poisson request rates (req/s)")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="serving: arrivals per rate")
+    ap.add_argument("--leg-rate", type=float, default=50.0, help="scale: request rate of the serving leg")
+    ap.add_argument("--leg-seconds", type=float, default=3.0, help="scale: arrivals of the serving leg")
+    ap.add_argument("--no-legs", action="store_true", help="scale: skip the batching and serving legs")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: default kernel config, no L2-flush buffer, no e2e/plain/CPU legs")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--prepare-reference", metavar="DIR", help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.prepare_reference:
+        prepare_reference_inputs(args.config, args.prepare_reference)
+        return
     if args.warmup < 3:
         log("[bench] warmup raised to 3")
         args.warmup = 3

@@ -12,7 +12,10 @@
  *   - plain pointers and sizes; device buffers are raw CUDA device pointers,
  *     streams are cudaStream_t passed as void*; the caller owns every buffer;
  *   - a scene handle may be used from several threads; calls on one handle
- *     that write the same output buffers must be ordered by the caller.
+ *     that write the same output buffers must be ordered by the caller;
+ *   - every call on a scene runs on the device the scene was created on
+ *     (the call makes it current and restores the caller's device after), so
+ *     output buffers and streams must belong to that device.
  */
 #ifndef KDGR_H_
 #define KDGR_H_
@@ -256,10 +259,12 @@ int kdgr_render_batch(kdgr_scene_t scene, const kdgr_view* views, int n_views, f
  * enter the allocator).  No counterpart in the reference.  Same kernel and
  * results as kdgr_render_batch, but the scratch (view table + work-queue
  * counter) is a fixed 32 KiB file-scope device array, so at most 256 views
- * per call (KDGR_ERR_LIMIT beyond); it calls no device allocator.  The first
- * call on a device looks up the array's device address -- make it before any
- * stream capture.  Calls share the array: calls that overlap on the GPU race;
- * issue them on one stream.  Asynchronous on `stream`. */
+ * per call (KDGR_ERR_LIMIT beyond); it calls no device allocator.  The view
+ * table reaches the array inside the parameters of a small staging kernel,
+ * so nothing enqueued refers to host memory after the call returns.  The
+ * first call on a device looks up the array's device address -- make it
+ * before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race; issue them on one stream.  Asynchronous on `stream`. */
 int kdgr_render_batch_noalloc(kdgr_scene_t scene, const kdgr_view* views, int n_views, float* d_rgb,
                               float* d_alpha, float* d_depth, const kdgr_batch_config* cfg, void* stream);
 

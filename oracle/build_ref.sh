@@ -10,16 +10,17 @@
 # does.
 #
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]
-#   REFERENCE_ROOT defaults to /root/reference.  The script exits 0 and
-#   builds nothing when that tree is absent (the prebuilt binary, if any, is
-#   used instead).
+#   The reference checkout comes from the argument or, without one, from the
+#   KDGR_REFERENCE_ROOT environment variable.  The script exits 0 and builds
+#   nothing when neither names a tree holding the builder sources (the
+#   prebuilt binary, if any, is used instead).
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${KDGR_REFERENCE_ROOT:-}}"
 KC="$REF/Kd-treeConverter_v0.9/Kd-treeConverter"
 OUT="$HERE/_ref"
-if [ ! -f "$KC/Kd-treeConstructor.cpp" ]; then
-  echo "build_ref: reference sources not present at $KC; skipped"
+if [ -z "$REF" ] || [ ! -f "$KC/Kd-treeConstructor.cpp" ]; then
+  echo "build_ref: reference sources not given or not present (argument or KDGR_REFERENCE_ROOT); skipped"
   exit 0
 fi
 mkdir -p "$OUT"

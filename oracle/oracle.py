@@ -180,6 +180,32 @@ def render_hybrid(scene: OracleScene, cam, width: int, height: int, spheres=(), 
     return rgb
 
 
+def read_kdt(path: str):
+    """read_kd_tree_from_file(obj, path, KD_TREE_DUMP_IN_BINARY)
+    (Kd-treeConverter.cpp:444-495) restated in numpy: f32 version (0.1),
+    f32 aabb[6] (xmin, ymin, zmin, xmax, ymax, zmax), i32 node count, 8-byte
+    nodes, i32 offset count, u32 offsets.  Returns (nodes (n, 2) uint32,
+    offsets uint32, aabb float32[6]).  Lets a checker load a tree without
+    the product library."""
+    raw = open(path, "rb").read()
+    hdr = np.frombuffer(raw, dtype="<f4", count=7)
+    if hdr[0] != np.float32(0.1):
+        raise ValueError(f"{path}: unsupported .kdt version {hdr[0]}")
+    pos = 28
+    nn = int(np.frombuffer(raw, dtype="<i4", count=1, offset=pos)[0])
+    pos += 4
+    if nn <= 0 or pos + 8 * nn + 4 > len(raw):
+        raise ValueError(f"{path}: bad node count {nn}")
+    nodes = np.frombuffer(raw, dtype="<u4", count=2 * nn, offset=pos).reshape(nn, 2).copy()
+    pos += 8 * nn
+    no = int(np.frombuffer(raw, dtype="<i4", count=1, offset=pos)[0])
+    pos += 4
+    if no < 0 or pos + 4 * no > len(raw):
+        raise ValueError(f"{path}: bad offset count {no}")
+    offsets = np.frombuffer(raw, dtype="<u4", count=no, offset=pos).copy()
+    return nodes, offsets, hdr[1:7].astype(np.float32)
+
+
 def to_image(values: np.ndarray, width: int, height: int) -> np.ndarray:
     """Arrange per-pixel values of a full render (pixel y*width+x in kernel
     row order) into the reference's framebuffer layout, rows flipped

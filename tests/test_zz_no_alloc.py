@@ -8,8 +8,13 @@ instead of the allocator.  Called here through the C ABI, twice in a row with
 different view sets -- the shared array keeps the previous call's contents,
 so each call must rewrite the table and zero the counter -- and checked
 against kdgr_render_batch within the parity tolerance of the tests (1e-5
-absolute).  The file sorts last so that a run stopping at the first failure
-has already run every other test; it also passes alone in a fresh process.
+absolute).  A third test checks the defining property itself: around a
+warmed-up call, the high-water mark of the device's default stream-ordered
+pool (the one kdgr_render_batch draws from) does not rise and the device's
+free memory does not change, while the same probe does see
+kdgr_render_batch's allocation.  The file sorts last so that a run stopping
+at the first failure has already run every other test; it also passes alone
+in a fresh process.
 """
 import ctypes
 
@@ -57,6 +62,68 @@ def test_noalloc_matches_batch_two_calls(pkg, cuda, fixtures):
         np.testing.assert_allclose(rgb.cpu().numpy(), ref_rgb.cpu().numpy(), rtol=0, atol=TOL)
         np.testing.assert_allclose(alpha.cpu().numpy(), ref_a.cpu().numpy(), rtol=0, atol=TOL)
         assert float(ref_a.max()) > 0.0  # the views see the scene
+    scene.close()
+
+
+# CUmemPool_attribute values (cuda.h)
+_USED_MEM_CURRENT = 7
+_USED_MEM_HIGH = 8
+
+
+class _DefaultPool:
+    """High-water mark of the current device's default memory pool, read
+    through the driver API (libcuda), reset before each probe."""
+
+    def __init__(self, index):
+        cu = ctypes.CDLL("libcuda.so.1")
+        dev = ctypes.c_int()
+        assert cu.cuDeviceGet(ctypes.byref(dev), index) == 0
+        self.pool = ctypes.c_void_p()
+        assert cu.cuDeviceGetDefaultMemPool(ctypes.byref(self.pool), dev) == 0
+        self.cu = cu
+
+    def _attr(self, a):
+        v = ctypes.c_uint64()
+        assert self.cu.cuMemPoolGetAttribute(self.pool, a, ctypes.byref(v)) == 0
+        return v.value
+
+    def reset(self):
+        zero = ctypes.c_uint64(0)
+        assert self.cu.cuMemPoolSetAttribute(self.pool, _USED_MEM_HIGH, ctypes.byref(zero)) == 0
+        return self._attr(_USED_MEM_CURRENT)
+
+    def high(self):
+        return self._attr(_USED_MEM_HIGH)
+
+
+def test_noalloc_takes_no_device_memory(pkg, cuda, fixtures):
+    F = pkg.renderer
+    fx = fixtures["cluster2k"]
+    scene = F.Scene(fx.tree, fx.rec)
+    fn = _noalloc(pkg)
+    stream = torch.cuda.current_stream().cuda_stream
+    cams = pkg.scenes.sphere_cameras(4, seed=23, resolutions=[(40, 32)])
+    views, total, _ = F.make_views(cams)
+    rgb = torch.zeros(total * 3, device=cuda)
+    ref = torch.zeros(total * 3, device=cuda)
+    pool = _DefaultPool(cuda.index)
+    for _ in range(2):  # warm-up: modules loaded, scratch address looked up
+        assert fn(scene.handle, views, len(cams), rgb.data_ptr(), None, None, None, stream) == 0
+        scene.render_batch(views, len(cams), ref)
+    torch.cuda.synchronize()
+    # positive control: the allocating entry point raises the pool's high-water mark
+    base = pool.reset()
+    scene.render_batch(views, len(cams), ref)
+    torch.cuda.synchronize()
+    assert pool.high() > base
+    free0 = torch.cuda.mem_get_info(cuda)[0]
+    base = pool.reset()
+    rc = fn(scene.handle, views, len(cams), rgb.data_ptr(), None, None, None, stream)
+    assert rc == 0, pkg.capi.lib().kdgr_last_error()
+    torch.cuda.synchronize()
+    assert pool.high() == base
+    assert torch.cuda.mem_get_info(cuda)[0] == free0
+    np.testing.assert_allclose(rgb.cpu().numpy(), ref.cpu().numpy(), rtol=0, atol=TOL)
     scene.close()
 
 
