@@ -144,3 +144,51 @@ def miss():
     """Camera looking away from the scene box."""
     tree, rec, _ = analytic_single()
     return tree, rec, sc.look_at((0.0, 0.0, 2.5), target=(0.0, 0.0, 5.0), aspect=1.0)
+
+
+# ---------------------------------------------------------------- pins
+# Scenes whose expected images come from mathematics written independently of
+# the oracle (tests/closed_form.py): one SH basis function at a time, a row
+# of Gaussians composited front to back, and opacity reaching exactly 0.99.
+
+def sh_probe(k: int, channel: int, coef: float):
+    """One isotropic Gaussian at the origin whose only colour term is SH
+    basis function k (1..15) of `channel` (DC coefficients zero), seen by
+    six wide-angle cameras around it, so the ray directions cover the
+    sphere.  Returns (tree, rec, [(camera, W, H)])."""
+    rest = np.zeros(45, np.float32)
+    rest[channel * 15 + (k - 1)] = coef  # f_rest is channel-major (cudaRenderer.cu:498)
+    g = gaussian((0.0, 0.0, 0.0), (0.35, 0.35, 0.35), opacity=0.9, dc=(0.0, 0.0, 0.0), rest=rest)
+    tree, rec = single([g])
+    eyes = [(0, 0, 1.2), (0, 0, -1.2), (1.2, 0, 0), (-1.2, 0, 0), (0.7, 0.7, 0.7), (-0.6, -0.8, 0.5)]
+    cams = [(sc.look_at(e, fovy=70.0, aspect=1.0), 20, 20) for e in eyes]
+    return tree, rec, cams
+
+
+def row(order=(3, 0, 4, 1, 2)):
+    """Five small isotropic Gaussians on the view axis at z = 0.6, 0.3, 0,
+    -0.3, -0.6 (front to back from the camera at z = 2.5), listed in one
+    leaf in a shuffled order: opacities 0.5, 0.7, 0.003 (alpha always below
+    1/255: skipped), 1.0 (alpha capped at 0.99 near the axis), 0.6."""
+    zs = [0.6, 0.3, 0.0, -0.3, -0.6]
+    ops = [0.5, 0.7, 0.003, 1.0, 0.6]
+    dcs = [(0.9, 0.1, 0.2), (0.2, 0.8, 0.1), (0.5, 0.5, 0.5), (0.1, 0.3, 0.9), (0.7, 0.6, 0.0)]
+    gs = [gaussian((0.0, 0.0, z), (0.05, 0.05, 0.05), opacity=o, dc=c) for z, o, c in zip(zs, ops, dcs)]
+    tree = make_tree([leaf(5, 0)], list(order), (-1, -1, -1, 1, 1, 1))
+    return tree, np.stack(gs), sc.front_camera(32, 32, fovy=6.0)
+
+
+def exact_099(split: bool):
+    """Gaussian P (opacity 1, z = 0.3) in front of Q (opacity 0.5, z = -0.3).
+    Near the axis P's alpha is capped at exactly 0.99, so the accumulated
+    opacity reaches exactly 0.99 after P.  Inside a leaf the walk stops only
+    when it exceeds 0.99, so with both in one leaf Q is still composited; at a
+    leaf boundary it stops once it reaches 0.99, so with a split plane at
+    z = 0 between them (split=True) Q is not."""
+    gp = gaussian((0.0, 0.0, 0.3), (0.05, 0.05, 0.05), opacity=1.0, dc=(0.9, 0.2, 0.1))
+    gq = gaussian((0.0, 0.0, -0.3), (0.05, 0.05, 0.05), opacity=0.5, dc=(0.1, 0.9, 0.4))
+    if split:
+        tree = make_tree([inner(2, 1, 0.0), leaf(1, 0), leaf(1, 1)], [1, 0], (-1, -1, -1, 1, 1, 1))
+    else:
+        tree = make_tree([leaf(2, 0)], [0, 1], (-1, -1, -1, 1, 1, 1))
+    return tree, np.stack([gp, gq]), sc.front_camera(24, 24, fovy=4.0)
