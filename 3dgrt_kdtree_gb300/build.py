@@ -29,6 +29,7 @@ CU_UNITS = {
     "render_exact.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "render_fast.cu": [],
     "kdgr_noalloc.cu": [],
+    "scene_pack.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "kdbuild_gpu.cu": ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"],
 }
 CPP_UNITS = ["kdbuild.cpp", "kdgr_tree_api.cpp", "kdgr_api.cpp", "kdgr_batch_api.cpp", "kdgr_reference_api.cpp",

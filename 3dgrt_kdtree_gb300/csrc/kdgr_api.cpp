@@ -168,23 +168,131 @@ namespace {
 
 constexpr int kTopLevels = 10;  // 2047 nodes at most = 16 KB of shared memory
 
-// R^T of quaternionWXYZToMatrixTranspose (cudaRenderer.cu:808-828) in double.
-void quat_rt_d(const float* q, double m[3][3]) {
-  const double r = q[0], x = q[1], y = q[2], z = q[3];
-  const double xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
-  const double rx = r * x, ry = r * y, rz = r * z;
-  m[0][0] = 1 - 2 * (yy + zz);
-  m[0][1] = 2 * (xy + rz);
-  m[0][2] = 2 * (xz - ry);
-  m[1][0] = 2 * (xy - rz);
-  m[1][1] = 1 - 2 * (xx + zz);
-  m[1][2] = 2 * (yz + rx);
-  m[2][0] = 2 * (xz + ry);
-  m[2][1] = 2 * (yz - rx);
-  m[2][2] = 1 - 2 * (xx + yy);
+}  // namespace
+
+namespace kdgr {
+
+// renderGaussianWithCudaSetup (cudaRenderer.cu:2557-2703) from device-resident
+// 64-float records: the per-Gaussian arrays of every requested form are
+// written by the packing kernel (scene_pack.cu), the tree is uploaded as
+// given (plain form) and relaid out with its leaf-order pair records (fast
+// forms).  The tree must have been validated.
+int scene_create_impl(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
+                      const float aabb[6], const float* d_g, uint32_t n, uint32_t flags, uint32_t depth,
+                      kdgr_scene_t* out, const char* who) {
+  const std::string w(who);
+  uint32_t forms = flags & (KDGR_FORM_EXACT | KDGR_FORM_FAST | KDGR_FORM_PACKED);
+  if (forms == 0) forms = KDGR_FORM_EXACT | KDGR_FORM_FAST;
+  const bool inverted = (flags & KDGR_SCALES_INVERTED) != 0;
+
+  std::unique_ptr<kdgr_scene_s> s(new kdgr_scene_s);
+  cudaGetDevice(&s->device);
+  s->forms = forms;
+  s->n_nodes = n_nodes;
+  s->n_offsets = n_offsets;
+  s->n_gauss = n;
+  s->depth = depth;
+  memcpy(s->aabb, aabb, sizeof(s->aabb));
+  for (uint32_t i = 0; i < n_nodes; ++i)
+    if ((nodes[2 * i] & 7u) == 3u) {
+      ++s->n_leaves;
+      if ((nodes[2 * i] >> 3) > s->max_leaf) s->max_leaf = nodes[2 * i] >> 3;
+    }
+
+  DevAlloc A;
+  std::vector<void*> staging;
+  auto fail = [&](const std::string& where, cudaError_t e = cudaSuccess) {
+    if (e == cudaSuccess) e = A.err != cudaSuccess ? A.err : cudaGetLastError();
+    for (void* p : staging) cudaFree(p);
+    A.release();
+    return cuda_fail(e, (w + ": " + where).c_str());
+  };
+  auto stage = [&](size_t bytes, void** p) {
+    const cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e == cudaSuccess) staging.push_back(*p);
+    return e;
+  };
+  s->d_offsets = A.alloc<uint32_t>(n_offsets ? n_offsets : 1);
+  s->d_sh = A.alloc<float4>(12 * (size_t)n);
+  s->d_status = A.alloc<uint32_t>(1);
+  if (forms & KDGR_FORM_EXACT) {
+    s->d_nodes = A.alloc<uint2>(n_nodes);
+    s->d_test = A.alloc<float4>(4 * (size_t)n);
+  }
+  if (forms & (KDGR_FORM_FAST | KDGR_FORM_PACKED)) s->d_opacity = A.alloc<float>(n);
+  if (forms & KDGR_FORM_PACKED) s->d_sh_bf16 = A.alloc<uint4>(6 * (size_t)n);
+  if (A.err != cudaSuccess) return fail("cudaMalloc");
+  if (n_offsets && cudaMemcpy(s->d_offsets, offsets, 4ull * n_offsets, cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail("upload offsets");
+  if (s->d_nodes && cudaMemcpy(s->d_nodes, nodes, 8ull * n_nodes, cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail("upload nodes");
+  if (cudaMemset(s->d_status, 0, 4) != cudaSuccess) return fail("status");
+
+  // per-Gaussian arrays, packed on the device
+  PackOut po{};
+  po.sh = s->d_sh;
+  po.test = s->d_test;
+  po.opacity = s->d_opacity;
+  po.sh_bf16 = s->d_sh_bf16;
+  float* d_giscl = nullptr;
+  float4* d_fast = nullptr;
+  uint32_t* d_packed = nullptr;
+  uint8_t* d_aniso = nullptr;
+  cudaError_t e = stage(12ull * n, (void**)&d_giscl);
+  if (e == cudaSuccess && (forms & KDGR_FORM_FAST)) e = stage(48ull * n, (void**)&d_fast);
+  if (e == cudaSuccess && (forms & KDGR_FORM_PACKED)) e = stage(32ull * n, (void**)&d_packed);
+  if (e == cudaSuccess && (forms & KDGR_FORM_PACKED)) e = stage(n, (void**)&d_aniso);
+  if (e != cudaSuccess) return fail("cudaMalloc (staging)", e);
+  po.giscl = d_giscl;
+  po.fast = d_fast;
+  po.packed = d_packed;
+  po.aniso = d_aniso;
+  e = launch_pack(d_g, n, inverted, po, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return fail("packing kernel", e);
+
+  std::vector<uint32_t> relaid, pair_gid;  // relaid fast tree, padded leaf order (fast forms)
+  if (forms & (KDGR_FORM_FAST | KDGR_FORM_PACKED)) {
+    relayout_tree(nodes, n_nodes, kTopLevels, relaid, &s->top_nodes);
+    pad_leaf_pairs(relaid, offsets, pair_gid);
+    if (pair_gid.size() > 0xFFFFFFF0ull) {
+      for (void* p : staging) cudaFree(p);
+      A.release();
+      set_error(w + ": more than 2^32 leaf entries after pair padding");
+      return KDGR_ERR_LIMIT;
+    }
+    s->n_pair_entries = (uint32_t)pair_gid.size();
+    s->d_nodes_fast = A.alloc<uint2>(n_nodes);
+    s->d_pair_gid = A.alloc<uint32_t>(pair_gid.size() + 2);
+    if (A.err != cudaSuccess) return fail("cudaMalloc (tree)");
+    if (cudaMemcpy(s->d_nodes_fast, relaid.data(), 8ull * n_nodes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (!pair_gid.empty() && cudaMemcpy(s->d_pair_gid, pair_gid.data(), 4 * pair_gid.size(),
+                                         cudaMemcpyHostToDevice) != cudaSuccess))
+      return fail("upload (tree)");
+  }
+  if (forms & KDGR_FORM_FAST) {
+    // the per-Gaussian rows are staging: the kernels read the leaf-order pairs
+    s->d_leaf_pairs = A.alloc<float4>(6 * ((size_t)s->n_pair_entries / 2 + 1));
+    if (A.err != cudaSuccess) return fail("cudaMalloc (fast)");
+    e = build_leaf_pairs(s->d_pair_gid, s->n_pair_entries, d_fast, s->d_leaf_pairs);
+    if (e != cudaSuccess) return fail("leaf pairs (fast)", e);
+  }
+  if (forms & KDGR_FORM_PACKED) {
+    const int rc = pack_precision(s.get(), d_g, d_giscl, d_packed, d_aniso, relaid, pair_gid, A);
+    if (rc != KDGR_OK) {
+      for (void* p : staging) cudaFree(p);
+      A.release();
+      return rc;
+    }
+  }
+  for (void* p : staging) cudaFree(p);
+  s->device_bytes = A.bytes;
+  A.ptrs.clear();  // ownership moves to the scene
+  *out = s.release();
+  return KDGR_OK;
 }
 
-}  // namespace
+}  // namespace kdgr
 
 extern "C" {
 
@@ -216,143 +324,36 @@ int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* o
     set_error("kdgr_scene_create: " + err);
     return rc;
   }
-  uint32_t forms = flags & (KDGR_FORM_EXACT | KDGR_FORM_FAST | KDGR_FORM_PACKED);
-  if (forms == 0) forms = KDGR_FORM_EXACT | KDGR_FORM_FAST;
-  const bool inverted = (flags & KDGR_SCALES_INVERTED) != 0;
+  // the records go to the device as they are; the device packs every form
+  float* d_rec = nullptr;
+  cudaError_t e = cudaMalloc(&d_rec, 256ull * n);
+  if (e == cudaSuccess) e = cudaMemcpy(d_rec, g, 256ull * n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (d_rec) cudaFree(d_rec);
+    return cuda_fail(e, "kdgr_scene_create: record upload");
+  }
+  rc = scene_create_impl(nodes, n_nodes, offsets, n_offsets, aabb, d_rec, n, flags, depth, out,
+                         "kdgr_scene_create");
+  cudaFree(d_rec);
+  return rc;
+}
 
-  std::unique_ptr<kdgr_scene_s> s(new kdgr_scene_s);
-  cudaGetDevice(&s->device);
-  s->forms = forms;
-  s->n_nodes = n_nodes;
-  s->n_offsets = n_offsets;
-  s->n_gauss = n;
-  s->depth = depth;
-  memcpy(s->aabb, aabb, sizeof(s->aabb));
-  for (uint32_t i = 0; i < n_nodes; ++i)
-    if ((nodes[2 * i] & 7u) == 3u) {
-      ++s->n_leaves;
-      if ((nodes[2 * i] >> 3) > s->max_leaf) s->max_leaf = nodes[2 * i] >> 3;
-    }
-
-  // host-side layouts
-  std::vector<float> giscl(3 * (size_t)n);
-  for (size_t i = 0; i < n; ++i)
-    for (int c = 0; c < 3; ++c) {
-      const float sc = g[64 * i + 4 + c];
-      giscl[3 * i + c] = inverted ? sc : 1 / sc;  // the caller-side inversion, FP32
-    }
-  std::vector<float> sh(48 * (size_t)n);
-  for (size_t i = 0; i < n; ++i) {
-    const float* r = g + 64 * i;
-    for (int c = 0; c < 3; ++c) sh[48 * i + c] = r[12 + c];
-    for (int k = 1; k < 16; ++k)
-      for (int c = 0; c < 3; ++c) sh[48 * i + 3 * k + c] = r[15 + 15 * c + (k - 1)];
+int kdgr_scene_create_device(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
+                             const float aabb[6], const float* d_g, uint32_t n, uint32_t flags, kdgr_scene_t* out) {
+  if (!out || !nodes || !aabb || !d_g || n == 0 || n_nodes == 0 || (n_offsets && !offsets)) {
+    set_error("kdgr_scene_create_device: null argument, no nodes or no Gaussians");
+    return KDGR_ERR_INVALID_ARG;
   }
-
-  DevAlloc A;
-  auto fail = [&](const char* where) {
-    const cudaError_t e = A.err != cudaSuccess ? A.err : cudaGetLastError();
-    A.release();
-    return cuda_fail(e, where);
-  };
-  s->d_offsets = A.alloc<uint32_t>(n_offsets ? n_offsets : 1);
-  s->d_sh = A.alloc<float4>(12 * (size_t)n);
-  s->d_status = A.alloc<uint32_t>(1);
-  if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc");
-  if (n_offsets && cudaMemcpy(s->d_offsets, offsets, 4ull * n_offsets, cudaMemcpyHostToDevice) != cudaSuccess)
-    return fail("kdgr_scene_create: upload offsets");
-  if (cudaMemcpy(s->d_sh, sh.data(), sh.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
-    return fail("kdgr_scene_create: upload SH");
-  if (cudaMemset(s->d_status, 0, 4) != cudaSuccess) return fail("kdgr_scene_create: status");
-
-  if (forms & KDGR_FORM_EXACT) {
-    std::vector<float> te(16 * (size_t)n, 0.f);
-    for (size_t i = 0; i < n; ++i) {
-      const float* r = g + 64 * i;
-      float* t = te.data() + 16 * i;
-      t[0] = r[0];
-      t[1] = r[1];
-      t[2] = r[2];
-      t[3] = r[3];
-      t[4] = giscl[3 * i];
-      t[5] = giscl[3 * i + 1];
-      t[6] = giscl[3 * i + 2];
-      t[7] = 1 / giscl[3 * i];      // particleScale = 1 / giscl, cudaRenderer.cu:1091
-      t[8] = 1 / giscl[3 * i + 1];
-      t[9] = 1 / giscl[3 * i + 2];
-      t[10] = r[8];
-      t[11] = r[9];
-      t[12] = r[10];
-      t[13] = r[11];
-    }
-    s->d_nodes = A.alloc<uint2>(n_nodes);
-    s->d_test = A.alloc<float4>(4 * (size_t)n);
-    if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (exact)");
-    if (cudaMemcpy(s->d_nodes, nodes, 8ull * n_nodes, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(s->d_test, te.data(), te.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
-      return fail("kdgr_scene_create: upload (exact)");
+  *out = nullptr;
+  std::string err;
+  uint32_t depth = 0;
+  int rc = validate_tree(nodes, n_nodes, offsets, n_offsets, n, err, &depth);
+  if (rc != KDGR_OK) {
+    set_error("kdgr_scene_create_device: " + err);
+    return rc;
   }
-  std::vector<uint32_t> relaid, pair_gid;  // relaid fast tree, padded leaf order (fast forms)
-  if (forms & (KDGR_FORM_FAST | KDGR_FORM_PACKED)) {
-    relayout_tree(nodes, n_nodes, kTopLevels, relaid, &s->top_nodes);
-    pad_leaf_pairs(relaid, offsets, pair_gid);
-    if (pair_gid.size() > 0xFFFFFFF0ull) {
-      A.release();
-      set_error("kdgr_scene_create: more than 2^32 leaf entries after pair padding");
-      return KDGR_ERR_LIMIT;
-    }
-    s->n_pair_entries = (uint32_t)pair_gid.size();
-    s->d_nodes_fast = A.alloc<uint2>(n_nodes);
-    s->d_pair_gid = A.alloc<uint32_t>(pair_gid.size() + 2);
-    if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (tree)");
-    if (cudaMemcpy(s->d_nodes_fast, relaid.data(), 8ull * n_nodes, cudaMemcpyHostToDevice) != cudaSuccess ||
-        (!pair_gid.empty() && cudaMemcpy(s->d_pair_gid, pair_gid.data(), 4 * pair_gid.size(),
-                                         cudaMemcpyHostToDevice) != cudaSuccess))
-      return fail("kdgr_scene_create: upload (tree)");
-  }
-  if (forms & KDGR_FORM_FAST) {
-    // rows of M = diag(1/s) R^T and b = M mu, in FP64, stored FP32
-    std::vector<float> tf(12 * (size_t)n), op(n);
-    for (size_t i = 0; i < n; ++i) {
-      const float* r = g + 64 * i;
-      double m[3][3];
-      quat_rt_d(r + 8, m);
-      float* t = tf.data() + 12 * i;
-      for (int row = 0; row < 3; ++row) {
-        const double sc = giscl[3 * i + row];
-        double b = 0;
-        for (int c = 0; c < 3; ++c) {
-          const double mv = sc * m[row][c];
-          t[4 * row + c] = (float)mv;
-          b += mv * (double)r[c];
-        }
-        t[4 * row + 3] = (float)b;
-      }
-      op[i] = r[3];
-    }
-    s->d_opacity = A.alloc<float>(n);
-    s->d_leaf_pairs = A.alloc<float4>(6 * ((size_t)s->n_pair_entries / 2 + 1));
-    if (A.err != cudaSuccess) return fail("kdgr_scene_create: cudaMalloc (fast)");
-    // the per-Gaussian records are staging only: the kernels read the leaf-order pairs
-    float4* d_stage = nullptr;
-    cudaError_t e = cudaMalloc(&d_stage, tf.size() * 4);
-    if (e == cudaSuccess) e = cudaMemcpy(d_stage, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(s->d_opacity, op.data(), op.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = build_leaf_pairs(s->d_pair_gid, s->n_pair_entries, d_stage, s->d_leaf_pairs);
-    if (d_stage) cudaFree(d_stage);
-    if (e != cudaSuccess) return fail("kdgr_scene_create: upload (fast)");
-  }
-  if (forms & KDGR_FORM_PACKED) {
-    rc = pack_precision(s.get(), g, giscl.data(), sh.data(), relaid, pair_gid, A);
-    if (rc != KDGR_OK) {
-      A.release();
-      return rc;
-    }
-  }
-  s->device_bytes = A.bytes;
-  A.ptrs.clear();  // ownership moves to the scene
-  *out = s.release();
-  return KDGR_OK;
+  return scene_create_impl(nodes, n_nodes, offsets, n_offsets, aabb, d_g, n, flags, depth, out,
+                           "kdgr_scene_create_device");
 }
 
 int kdgr_scene_destroy(kdgr_scene_t s) {

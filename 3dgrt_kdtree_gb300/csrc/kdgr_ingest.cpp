@@ -36,6 +36,7 @@
 
 #include "kdgr.h"
 #include "kdgr_internal.h"
+#include "scene.h"
 
 namespace kdgr {
 namespace {
@@ -93,14 +94,10 @@ void activate(const uint8_t* v, const int off[16], float* r) {
     for (int i = 0; i < 45; ++i) r[15 + i] = f(off[14] + 4 * i);
 }
 
-int read_ply(const char* path, std::vector<float>& rec, uint32_t& n_out, std::string& err) {
-  FILE* fp = fopen(path, "rb");
-  if (!fp) {
-    err = std::string("cannot open ") + path;
-    return KDGR_ERR_IO;
-  }
+}  // namespace
+
+int parse_ply_header(FILE* fp, PlyLayout& lay, uint64_t& n_out, uint32_t& stride_out, std::string& err) {
   auto fail = [&](const std::string& m, int code) {
-    fclose(fp);
     err = m;
     return code;
   };
@@ -153,14 +150,14 @@ int read_ply(const char* path, std::vector<float>& rec, uint32_t& n_out, std::st
 
   static const char* kNeed[14] = {"x",       "y",       "z",       "opacity", "scale_0", "scale_1", "scale_2",
                                   "rot_0",   "rot_1",   "rot_2",   "rot_3",   "f_dc_0",  "f_dc_1",  "f_dc_2"};
-  int off[16];
   for (int i = 0; i < 14; ++i) {
     auto it = props.find(kNeed[i]);
     if (it == props.end() || !it->second.is_float)
       return fail(std::string("missing float property '") + kNeed[i] + "'", KDGR_ERR_FORMAT);
-    off[i] = it->second.offset;
+    lay.off[i] = it->second.offset;
   }
-  off[14] = -1;
+  lay.off[14] = -1;
+  lay.off[15] = 0;
   auto r0 = props.find("f_rest_0");
   if (r0 != props.end()) {
     for (int k = 0; k < 45; ++k) {
@@ -168,19 +165,44 @@ int read_ply(const char* path, std::vector<float>& rec, uint32_t& n_out, std::st
       if (it == props.end() || !it->second.is_float || it->second.offset != r0->second.offset + 4 * k)
         return fail("f_rest_0..44 must be 45 consecutive floats", KDGR_ERR_FORMAT);
     }
-    off[14] = r0->second.offset;
+    lay.off[14] = r0->second.offset;
   }
+  n_out = (uint64_t)n_vertices;
+  stride_out = (uint32_t)stride;
+  return KDGR_OK;
+}
 
+namespace {
+
+int read_ply(const char* path, std::vector<float>& rec, uint32_t& n_out, std::string& err) {
+  FILE* fp = fopen(path, "rb");
+  if (!fp) {
+    err = std::string("cannot open ") + path;
+    return KDGR_ERR_IO;
+  }
+  PlyLayout lay;
+  uint64_t n_vertices = 0;
+  uint32_t stride = 0;
+  int rc = parse_ply_header(fp, lay, n_vertices, stride, err);
+  if (rc != KDGR_OK) {
+    fclose(fp);
+    return rc;
+  }
   const size_t n = (size_t)n_vertices;
   std::vector<uint8_t> raw;
   try {
     raw.resize(n * (size_t)stride);
     rec.assign(n * 64, 0.f);
   } catch (const std::bad_alloc&) {
-    return fail("host allocation failed for " + std::to_string(n) + " vertices", KDGR_ERR_OUT_OF_MEMORY);
+    fclose(fp);
+    err = "host allocation failed for " + std::to_string(n) + " vertices";
+    return KDGR_ERR_OUT_OF_MEMORY;
   }
-  if (fread(raw.data(), 1, raw.size(), fp) != raw.size())
-    return fail("vertex data shorter than the header announces", KDGR_ERR_FORMAT);
+  if (fread(raw.data(), 1, raw.size(), fp) != raw.size()) {
+    fclose(fp);
+    err = "vertex data shorter than the header announces";
+    return KDGR_ERR_FORMAT;
+  }
   fclose(fp);
 
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
@@ -189,7 +211,7 @@ int read_ply(const char* path, std::vector<float>& rec, uint32_t& n_out, std::st
   for (size_t b = 0; b < n; b += per) {
     const size_t e = std::min(n, b + per);
     pool.emplace_back([&, b, e] {
-      for (size_t i = b; i < e; ++i) activate(raw.data() + i * stride, off, rec.data() + 64 * i);
+      for (size_t i = b; i < e; ++i) activate(raw.data() + i * stride, lay.off, rec.data() + 64 * i);
     });
   }
   for (auto& t : pool) t.join();
@@ -231,4 +253,137 @@ extern "C" void kdgr_gaussians_free(kdgr_gaussians* g) {
   free(g->records);
   g->records = nullptr;
   g->n = 0;
+}
+
+namespace kdgr {
+namespace {
+
+// Stream the PLY vertex block to the device in chunks through two pinned
+// buffers, activating each chunk on the device while the next is read.
+int read_ply_device(const char* path, float* d_rec, uint32_t capacity, uint32_t* n_out, cudaStream_t st,
+                    std::string& err) {
+  FILE* fp = fopen(path, "rb");
+  if (!fp) {
+    err = std::string("cannot open ") + path;
+    return KDGR_ERR_IO;
+  }
+  PlyLayout lay;
+  uint64_t n = 0;
+  uint32_t stride = 0;
+  int rc = parse_ply_header(fp, lay, n, stride, err);
+  if (rc != KDGR_OK || !d_rec) {
+    fclose(fp);
+    if (rc == KDGR_OK) *n_out = (uint32_t)n;
+    return rc;
+  }
+  if (n > capacity) {
+    fclose(fp);
+    err = std::to_string(n) + " vertices exceed the capacity of " + std::to_string(capacity) + " records";
+    return KDGR_ERR_LIMIT;
+  }
+  const uint64_t per = std::max<uint64_t>(1, (16ull << 20) / stride);  // vertices per chunk (about 16 MB)
+  const size_t bytes = (size_t)per * stride;
+  uint8_t* host[2] = {nullptr, nullptr};
+  uint8_t* dev[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaError_t e = cudaSuccess;
+  for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+    e = cudaMallocHost(&host[b], bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&dev[b], bytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming);
+  }
+  uint64_t first = 0;
+  for (uint64_t c = 0; e == cudaSuccess && first < n; ++c) {
+    const int b = (int)(c & 1);
+    const uint64_t nv = std::min(per, n - first);
+    if (c >= 2) e = cudaEventSynchronize(ev[b]);  // the copy out of host[b] two chunks ago is done
+    if (e != cudaSuccess) break;
+    if (fread(host[b], 1, (size_t)nv * stride, fp) != (size_t)nv * stride) {
+      rc = KDGR_ERR_FORMAT;
+      err = "vertex data shorter than the header announces";
+      break;
+    }
+    e = cudaMemcpyAsync(dev[b], host[b], (size_t)nv * stride, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[b], st);
+    if (e == cudaSuccess) e = launch_ply_activate(dev[b], (uint32_t)nv, stride, lay, d_rec + 64ull * first, st);
+    first += nv;
+  }
+  const cudaError_t es = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = es;
+  for (int b = 0; b < 2; ++b) {
+    if (host[b]) cudaFreeHost(host[b]);
+    if (dev[b]) cudaFree(dev[b]);
+    if (ev[b]) cudaEventDestroy(ev[b]);
+  }
+  fclose(fp);
+  if (rc != KDGR_OK) return rc;
+  if (e != cudaSuccess) {
+    err = std::string("CUDA: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? KDGR_ERR_OUT_OF_MEMORY : KDGR_ERR_CUDA;
+  }
+  *n_out = (uint32_t)n;
+  return KDGR_OK;
+}
+
+}  // namespace
+}  // namespace kdgr
+
+extern "C" int kdgr_read_ply_device(const char* path, float* d_records, uint32_t capacity, uint32_t* n_out,
+                                    void* stream) {
+  if (!path || !n_out) {
+    set_error("kdgr_read_ply_device: null argument");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  std::string err;
+  const int rc = read_ply_device(path, d_records, capacity, n_out, (cudaStream_t)stream, err);
+  if (rc != KDGR_OK) set_error("kdgr_read_ply_device: " + err);
+  return rc;
+}
+
+extern "C" int kdgr_scene_create_from_files(const char* ply_path, const char* kdt_path, uint32_t flags,
+                                            kdgr_scene_t* out) {
+  if (!ply_path || !kdt_path || !out) {
+    set_error("kdgr_scene_create_from_files: null argument");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (flags & KDGR_SCALES_INVERTED) {
+    set_error("kdgr_scene_create_from_files: PLY records are activated, not inverted (drop KDGR_SCALES_INVERTED)");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  std::string err;
+  HostTree t;
+  int rc = read_kdt(kdt_path, t, err);
+  if (rc != KDGR_OK) {
+    set_error("kdgr_scene_create_from_files: " + err);
+    return rc;
+  }
+  uint32_t n = 0;
+  rc = read_ply_device(ply_path, nullptr, 0, &n, nullptr, err);  // vertex count from the header
+  if (rc != KDGR_OK) {
+    set_error("kdgr_scene_create_from_files: " + err);
+    return rc;
+  }
+  const uint32_t n_nodes = (uint32_t)(t.nodes.size() / 2), n_offsets = (uint32_t)t.offsets.size();
+  uint32_t depth = 0;
+  rc = validate_tree(t.nodes.data(), n_nodes, t.offsets.data(), n_offsets, n, err, &depth);
+  if (rc != KDGR_OK) {
+    set_error("kdgr_scene_create_from_files: " + err);
+    return rc;
+  }
+  float* d_rec = nullptr;
+  cudaError_t e = cudaMalloc(&d_rec, 256ull * n);
+  if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create_from_files: cudaMalloc");
+  uint32_t n2 = 0;
+  rc = read_ply_device(ply_path, d_rec, n, &n2, nullptr, err);
+  if (rc != KDGR_OK) {
+    cudaFree(d_rec);
+    set_error("kdgr_scene_create_from_files: " + err);
+    return rc;
+  }
+  rc = scene_create_impl(t.nodes.data(), n_nodes, t.offsets.data(), n_offsets, t.aabb, d_rec, n, flags, depth, out,
+                         "kdgr_scene_create_from_files");
+  cudaFree(d_rec);
+  return rc;
 }

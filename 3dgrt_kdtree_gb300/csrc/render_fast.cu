@@ -1115,70 +1115,22 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
   return cudaGetLastError();
 }
 
-int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh,
-                   const std::vector<uint32_t>& relaid, const std::vector<uint32_t>& pair_gid, DevAlloc& A) {
+// The precision form from the device packing kernel's outputs (d_packed:
+// FP32 mean + FP16 M per Gaussian; d_aniso: flagged Gaussians; BF16 SH and
+// opacity already in the scene): the flagged Gaussians get FP64-precomputed
+// factors (k_aniso_fp64) and each leaf is laid out as its plain entries in
+// FP16 pairs followed by its flagged entries in FP32 pairs of a second stream.
+int pack_precision(kdgr_scene_s* s, const float* d_rec, const float* d_giscl, const uint32_t* d_packed,
+                   const uint8_t* d_aniso, const std::vector<uint32_t>& relaid,
+                   const std::vector<uint32_t>& pair_gid, DevAlloc& A) {
   const size_t n = s->n_gauss;
-  std::vector<uint32_t> packed(8 * n);
-  std::vector<uint16_t> shb(48 * n);
+  std::vector<uint8_t> flag(n);
+  if (cudaMemcpy(flag.data(), d_aniso, n, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cuda_fail(cudaGetLastError(), "kdgr_scene_create: aniso flags");
   std::vector<uint32_t> aidx(n, 0xFFFFFFFFu);
-  std::vector<float> aniso_src;
   uint32_t n_aniso = 0;
-  auto pk = [](float a, float b) {
-    __half2 h = __floats2half2_rn(a, b);
-    uint32_t w;
-    memcpy(&w, &h, 4);
-    return w;
-  };
-  std::vector<float> opac(n);
-  for (size_t i = 0; i < n; ++i) {
-    const float* r = g + 64 * i;
-    const float* gs = giscl + 3 * i;
-    uint32_t* p = packed.data() + 8 * i;
-    const double smax = 1.0 / std::min(std::min((double)gs[0], (double)gs[1]), (double)gs[2]);
-    const double smin = 1.0 / std::max(std::max((double)gs[0], (double)gs[1]), (double)gs[2]);
-    // M = diag(1/s) R^T in FP64 (rows), then FP16
-    const double qr = r[8], qx = r[9], qy = r[10], qz = r[11];
-    const double xx = qx * qx, yy = qy * qy, zz = qz * qz, xy = qx * qy, xz = qx * qz, yz = qy * qz;
-    const double rx = qr * qx, ry = qr * qy, rz = qr * qz;
-    const double rt[3][3] = {{1 - 2 * (yy + zz), 2 * (xy + rz), 2 * (xz - ry)},
-                             {2 * (xy - rz), 1 - 2 * (xx + zz), 2 * (yz + rx)},
-                             {2 * (xz + ry), 2 * (yz - rx), 1 - 2 * (xx + yy)}};
-    float m[3][3];
-    double mmax = 0;
-    for (int row = 0; row < 3; ++row)
-      for (int c = 0; c < 3; ++c) {
-        const double v = (double)gs[row] * rt[row][c];
-        m[row][c] = (float)v;
-        mmax = std::max(mmax, std::fabs(v));
-      }
-    // very anisotropic Gaussians, and factors beyond the FP16 range, take the
-    // FP64-precomputed FP32 factors instead
-    const bool aniso = smax > kAnisoRatio * smin || mmax > 30000.0;
-    memcpy(&p[0], &r[0], 4);
-    memcpy(&p[1], &r[1], 4);
-    memcpy(&p[2], &r[2], 4);
-    p[3] = pk(m[2][2], 0.f);
-    p[4] = pk(m[0][0], m[0][1]);
-    p[5] = pk(m[0][2], m[1][0]);
-    p[6] = pk(m[1][1], m[1][2]);
-    p[7] = pk(m[2][0], m[2][1]);
-    opac[i] = r[3];
-    if (aniso) {
-      aidx[i] = n_aniso++;
-      const float src[10] = {gs[0], gs[1], gs[2], r[8], r[9], r[10], r[11], r[0], r[1], r[2]};
-      aniso_src.insert(aniso_src.end(), src, src + 10);
-    }
-    for (int k = 0; k < 48; ++k) {
-      __nv_bfloat16 b = __float2bfloat16_rn(sh[48 * i + k]);
-      memcpy(&shb[48 * i + k], &b, 2);
-    }
-  }
-  if (!s->d_opacity) {  // the FP32 form allocates it too
-    s->d_opacity = A.alloc<float>(n);
-    if (A.err == cudaSuccess &&
-        cudaMemcpy(s->d_opacity, opac.data(), n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
-      return cuda_fail(cudaErrorUnknown, "kdgr_scene_create: opacity upload (packed)");
-  }
+  for (size_t i = 0; i < n; ++i)
+    if (flag[i]) aidx[i] = n_aniso++;
   // The packed form's leaf layout: per leaf its plain entries in FP16 pairs,
   // then its flagged entries in FP32 pairs of a second stream, both padded
   // to whole pairs; the leaf words and per-node aux words say where.
@@ -1211,7 +1163,6 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
   s->n_plain_entries = (uint32_t)gid_plain.size();
   s->n_flag_entries = (uint32_t)gid_flag.size();
   s->n_aniso = n_aniso;
-  s->d_sh_bf16 = A.alloc<uint4>(6 * n);
   s->d_nodes_packed = A.alloc<uint2>(relaid.size() / 2);
   s->d_leaf_aux = A.alloc<uint2>(relaid.size() / 2);
   s->d_gid_plain = A.alloc<uint32_t>(gid_plain.size() + 2);
@@ -1219,27 +1170,23 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
   s->d_leaf_packed = A.alloc<uint4>(2 * (gid_plain.size() + 2));
   s->d_flag_pairs = A.alloc<float4>(3 * (gid_flag.size() + 2));
   if (A.err != cudaSuccess) return cuda_fail(A.err, "kdgr_scene_create: cudaMalloc (packed)");
-  // staging: per-Gaussian packed words, aniso index, FP64 precompute
-  uint32_t *d_stage = nullptr, *d_aidx = nullptr;
+  uint32_t* d_aidx = nullptr;
   float* d_src = nullptr;
   float4* d_table = nullptr;
   auto up = [](void* dst, const void* src, size_t bytes) {
     return bytes ? cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
   };
-  cudaError_t e = cudaMalloc(&d_stage, packed.size() * 4);
-  if (e == cudaSuccess) e = up(d_stage, packed.data(), packed.size() * 4);
-  if (e == cudaSuccess) e = up(s->d_sh_bf16, shb.data(), shb.size() * 2);
-  if (e == cudaSuccess) e = up(s->d_nodes_packed, nodes_p.data(), nodes_p.size() * 4);
+  cudaError_t e = up(s->d_nodes_packed, nodes_p.data(), nodes_p.size() * 4);
   if (e == cudaSuccess) e = up(s->d_leaf_aux, aux.data(), aux.size() * 4);
   if (e == cudaSuccess) e = up(s->d_gid_plain, gid_plain.data(), gid_plain.size() * 4);
   if (e == cudaSuccess) e = up(s->d_gid_flag, gid_flag.data(), gid_flag.size() * 4);
-  if (e == cudaSuccess) e = build_packed_pairs(s->d_gid_plain, s->n_plain_entries, d_stage, s->d_leaf_packed);
+  if (e == cudaSuccess) e = build_packed_pairs(s->d_gid_plain, s->n_plain_entries, d_packed, s->d_leaf_packed);
   if (e == cudaSuccess && n_aniso) {
-    e = cudaMalloc(&d_src, aniso_src.size() * 4);
+    e = cudaMalloc(&d_src, 40ull * n_aniso);
     if (e == cudaSuccess) e = cudaMalloc(&d_table, 3 * sizeof(float4) * n_aniso);
     if (e == cudaSuccess) e = cudaMalloc(&d_aidx, aidx.size() * 4);
-    if (e == cudaSuccess) e = up(d_src, aniso_src.data(), aniso_src.size() * 4);
     if (e == cudaSuccess) e = up(d_aidx, aidx.data(), aidx.size() * 4);
+    if (e == cudaSuccess) e = launch_gather_aniso(d_rec, d_giscl, d_aidx, (uint32_t)n, d_src, nullptr);
     if (e == cudaSuccess) {
       k_aniso_fp64<<<(n_aniso + 127) / 128, 128>>>(d_src, n_aniso, d_table);
       e = cudaGetLastError();
@@ -1247,7 +1194,7 @@ int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const fl
     if (e == cudaSuccess) e = build_flag_pairs(s->d_gid_flag, s->n_flag_entries, d_aidx, d_table, s->d_flag_pairs);
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
-  for (void* q : {(void*)d_stage, (void*)d_src, (void*)d_table, (void*)d_aidx})
+  for (void* q : {(void*)d_src, (void*)d_table, (void*)d_aidx})
     if (q) cudaFree(q);
   if (e != cudaSuccess) return cuda_fail(e, "kdgr_scene_create: packed upload");
   return KDGR_OK;

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdio>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -99,10 +100,11 @@ int cuda_fail(cudaError_t e, const char* where);
 // Fast-form tree relayout: top levels breadth-first, rest depth-first.
 void relayout_tree(const uint32_t* nodes, uint32_t n_nodes, int top_levels, std::vector<uint32_t>& out,
                    uint32_t* top_count);
-// Packed precision form: BF16 SH, FP16 inverse scales / quaternion /
-// opacity, and the FP64 upload-time factors of anisotropic Gaussians.
-int pack_precision(kdgr_scene_s* s, const float* g, const float* giscl, const float* sh,
-                   const std::vector<uint32_t>& relaid, const std::vector<uint32_t>& pair_gid, DevAlloc& A);
+// Packed precision form from the packing kernel's outputs: the FP64
+// upload-time factors of flagged Gaussians and the form's own leaf layout.
+int pack_precision(kdgr_scene_s* s, const float* d_rec, const float* d_giscl, const uint32_t* d_packed,
+                   const uint8_t* d_aniso, const std::vector<uint32_t>& relaid,
+                   const std::vector<uint32_t>& pair_gid, DevAlloc& A);
 // Fast-form leaf layout: rewrites the leaf words of the relaid tree
 // (y = first pair) and returns the padded per-entry Gaussian IDs.
 void pad_leaf_pairs(std::vector<uint32_t>& relaid, const uint32_t* offsets, std::vector<uint32_t>& pair_gid);
@@ -134,4 +136,38 @@ cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* 
                          uint32_t total_blocks, float* rgb, uint32_t* queue, uint32_t* status, cudaStream_t st);
 // Scale ratio above which a Gaussian's factors come from the FP64 precompute.
 constexpr double kAnisoRatio = 1e3;
+
+// Per-Gaussian outputs of the device packing kernel (scene_pack.cu); a null
+// pointer skips that output.
+struct PackOut {
+  float* giscl;         // 3 per Gaussian: inverse scale as uploaded by the reference's caller
+  float4* sh;           // 12 per Gaussian: FP32 SH, coefficient-major
+  float4* test;         // 4 per Gaussian: the plain kernel's test record
+  float4* fast;         // 3 per Gaussian: rows of M and b (FP64 -> FP32)
+  float* opacity;       // 1 per Gaussian
+  uint32_t* packed;     // 8 per Gaussian: FP32 mean + FP16 entries of M (precision form staging)
+  uint4* sh_bf16;       // 6 per Gaussian: BF16 SH, coefficient-major
+  uint8_t* aniso;       // 1 per Gaussian (with packed): takes the FP64-precomputed factors
+};
+cudaError_t launch_pack(const float* d_rec, uint32_t n, bool inverted, const PackOut& out, cudaStream_t st);
+// Fields of the FP64 precompute (k_aniso_fp64) for each flagged Gaussian i,
+// written to entry aidx[i] of d_out (10 floats each; aidx 0xFFFFFFFF skips).
+cudaError_t launch_gather_aniso(const float* d_rec, const float* d_giscl, const uint32_t* d_aidx, uint32_t n,
+                                float* d_out, cudaStream_t st);
+
+// Byte offsets within a PLY vertex of x, y, z, opacity, scale_0..2,
+// rot_0..3, f_dc_0..2 and f_rest_0 (-1 when the file has no f_rest).
+struct PlyLayout {
+  int off[16];
+};
+// Parse a 3DGS .ply header (binary little-endian, float fields found by
+// name); leaves fp at the first vertex.
+int parse_ply_header(FILE* fp, PlyLayout& lay, uint64_t& n_vertices, uint32_t& stride, std::string& err);
+cudaError_t launch_ply_activate(const uint8_t* d_raw, uint32_t n, uint32_t stride, const PlyLayout& lay,
+                                float* d_rec, cudaStream_t st);
+// Device records -> scene (all forms); the tree arrays are host arrays,
+// validated by the caller.
+int scene_create_impl(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
+                      const float aabb[6], const float* d_gaussians, uint32_t n, uint32_t flags, uint32_t depth,
+                      kdgr_scene_t* out, const char* who);
 }  // namespace kdgr

@@ -110,6 +110,10 @@ capi._EXTRA_SIGS.update({
     "kdgr_init": [ctypes.c_int],
     "kdgr_scene_create": [vp, ctypes.c_uint32, vp, ctypes.c_uint32, vp, vp, ctypes.c_uint32, ctypes.c_uint32,
                           ctypes.POINTER(vp)],
+    "kdgr_scene_create_device": [vp, ctypes.c_uint32, vp, ctypes.c_uint32, vp, vp, ctypes.c_uint32,
+                                 ctypes.c_uint32, ctypes.POINTER(vp)],
+    "kdgr_scene_create_from_files": [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32, ctypes.POINTER(vp)],
+    "kdgr_read_ply_device": [ctypes.c_char_p, vp, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32), vp],
     "kdgr_scene_destroy": [vp],
     "kdgr_scene_info_get": [vp, ctypes.POINTER(SceneInfo)],
     "kdgr_scene_status": [vp, ctypes.POINTER(ctypes.c_uint32), ctypes.c_int],
@@ -241,6 +245,19 @@ def debug_report(trace, width: int, height: int, out_dir: Optional[str] = None,
     return out
 
 
+def read_ply_device(path: str, device=None):
+    """kdgr_read_ply_device: the activated (n, 64) float32 records of a 3DGS
+    .ply as a CUDA tensor, activated on the device."""
+    import torch
+    n = ctypes.c_uint32()
+    L = capi.lib()
+    capi.check(L.kdgr_read_ply_device(path.encode(), None, 0, ctypes.byref(n), None), "kdgr_read_ply_device")
+    out = torch.empty((n.value, 64), dtype=torch.float32, device=device or "cuda")
+    capi.check(L.kdgr_read_ply_device(path.encode(), _ptr(out), n.value, ctypes.byref(n), _stream(None)),
+               "kdgr_read_ply_device")
+    return out
+
+
 def make_views(cams: Sequence) -> tuple:
     """[(Camera, W, H)] -> (ctypes View array, total pixels, per-view offsets)."""
     arr = (View * len(cams))()
@@ -273,6 +290,42 @@ class Scene:
                                        ctypes.byref(h)), "kdgr_scene_create")
         self.handle = h
         self.n_gaussians = rec.shape[0]
+
+    @classmethod
+    def _adopt(cls, handle, n: int) -> "Scene":
+        sc = cls.__new__(cls)
+        sc.handle = handle
+        sc.n_gaussians = n
+        return sc
+
+    @classmethod
+    def from_device(cls, tree: KdTree, d_gaussians, forms: int = FORM_EXACT | FORM_FAST,
+                    scales_inverted: bool = False) -> "Scene":
+        """kdgr_scene_create_device: records already on the device, a CUDA
+        tensor of shape (n, 64) float32 (e.g. from read_ply_device)."""
+        nodes = np.ascontiguousarray(tree.nodes, dtype=np.uint32)
+        offs = np.ascontiguousarray(tree.offsets, dtype=np.uint32)
+        aabb = np.ascontiguousarray(tree.aabb, dtype=np.float32)
+        if d_gaussians.dim() != 2 or d_gaussians.shape[1] != 64:
+            raise ValueError("device records must be an (n, 64) float32 CUDA tensor")
+        h = ctypes.c_void_p()
+        flags = forms | (SCALES_INVERTED if scales_inverted else 0)
+        capi.check(capi.lib().kdgr_scene_create_device(
+            nodes.ctypes.data, nodes.shape[0], offs.ctypes.data if offs.size else None, offs.shape[0],
+            aabb.ctypes.data, _ptr(d_gaussians), d_gaussians.shape[0], flags, ctypes.byref(h)),
+            "kdgr_scene_create_device")
+        return cls._adopt(h, int(d_gaussians.shape[0]))
+
+    @classmethod
+    def from_files(cls, ply_path: str, kdt_path: str, forms: int = FORM_EXACT | FORM_FAST) -> "Scene":
+        """kdgr_scene_create_from_files: a 3DGS .ply activated on the device
+        and a binary .kdt tree."""
+        h = ctypes.c_void_p()
+        capi.check(capi.lib().kdgr_scene_create_from_files(ply_path.encode(), kdt_path.encode(), forms,
+                                                            ctypes.byref(h)), "kdgr_scene_create_from_files")
+        sc = cls._adopt(h, 0)
+        sc.n_gaussians = sc.info()["n_gaussians"]
+        return sc
 
     def info(self) -> dict:
         i = SceneInfo()

@@ -180,6 +180,33 @@ int kdgr_shutdown(void);
 int kdgr_scene_create(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
                       const float aabb[6], const float* gaussians, uint32_t n_gaussians, uint32_t flags,
                       kdgr_scene_t* out);
+/* kdgr_scene_create with the Gaussian records already in device memory
+ * (d_gaussians: n_gaussians 64-float records on the current device, e.g.
+ * from kdgr_read_ply_device); the tree arrays are host arrays, validated
+ * first.  kdgr_scene_create itself copies the host records to the device and
+ * continues here: every form's per-Gaussian arrays are packed by device
+ * kernels (renderGaussianWithCudaSetup, cudaRenderer.cu:2557-2703). */
+int kdgr_scene_create_device(const uint32_t* nodes, uint32_t n_nodes, const uint32_t* offsets, uint32_t n_offsets,
+                             const float aabb[6], const float* d_gaussians, uint32_t n_gaussians, uint32_t flags,
+                             kdgr_scene_t* out);
+
+/* loadGaussiansFromPly (Kd-treeConverterMain.cpp:1652-1769) on the device:
+ * the header is parsed on the host, the vertex block streams to the device
+ * in chunks through pinned buffers and is activated there (sigmoid opacity,
+ * exp scale, normalised quaternion, k_scale) into 64-float records at
+ * d_records, the same records as kdgr_read_ply.  With d_records null only
+ * *n_out is set (the vertex count, for sizing the buffer); a file with more
+ * than `capacity` vertices is KDGR_ERR_LIMIT.  Synchronises `stream`. */
+int kdgr_read_ply_device(const char* path, float* d_records, uint32_t capacity, uint32_t* n_out, void* stream);
+
+/* A scene straight from the reference's two files: the .ply activated on the
+ * device (kdgr_read_ply_device) and the binary .kdt (read_kd_tree_from_file,
+ * Kd-treeConverter.cpp:444-495) validated and uploaded into the device tree
+ * arrays; the per-Gaussian arrays are packed on the device.  flags as
+ * kdgr_scene_create without KDGR_SCALES_INVERTED (PLY records are
+ * activated). */
+int kdgr_scene_create_from_files(const char* ply_path, const char* kdt_path, uint32_t flags, kdgr_scene_t* out);
+
 /* cleanupCudaResources (cudaRenderer.cu) for one scene. */
 int kdgr_scene_destroy(kdgr_scene_t scene);
 int kdgr_scene_info_get(kdgr_scene_t scene, kdgr_scene_info* out);
