@@ -74,6 +74,7 @@ void kdgr_batch_config_default(kdgr_batch_config* c) {
   c->hit_buffer = 4;
   c->traversal = KDGR_TRAV_PACKET;
   c->tile_shape = KDGR_TILE_8X4;
+  c->rays_per_warp = 32;
 }
 
 int kdgr_render_batch(kdgr_scene_t s, const kdgr_view* views, int n_views, float* rgb, float* alpha, float* depth,
@@ -233,8 +234,8 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
   float best_ms = 1e30f;
   // stage 1: schedule x register cap x chunk with warp packets, 8x4 tiles
   // and the 4-entry hit buffer; stage 2: the winner with the 8-entry buffer
-  // (dense leaves re-scan less), with per-ray traversal, and with 4x8 and
-  // 16x2 warp tiles
+  // (dense leaves re-scan less), with per-ray traversal, with 4x8 and 16x2
+  // warp tiles, and with 16 or 8 rays per warp (either traversal)
   bool stage2 = false;
   for (size_t ci = 0; ci < cands.size() || !stage2; ++ci) {
     if (ci == cands.size()) {  // reached once: appends the stage-2 candidates
@@ -250,6 +251,18 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
           kdgr_batch_config ct = *best;
           ct.tile_shape = tile;
           cands.push_back(ct);
+        }
+      // fewer rays per warp (2 or 4 lanes sharing each ray), on warp strips,
+      // with either traversal
+      for (int trav : {KDGR_TRAV_PACKET, KDGR_TRAV_RAY})
+        for (int rpw : {16, 8}) {
+          kdgr_batch_config cg = *best;
+          cg.schedule = KDGR_SCHED_WARP_STRIPS;
+          cg.chunk = 1;
+          cg.traversal = trav;
+          cg.tile_shape = KDGR_TILE_8X4;
+          cg.rays_per_warp = rpw;
+          cands.push_back(cg);
         }
     }
     const kdgr_batch_config c = cands[ci];
@@ -271,8 +284,9 @@ int kdgr_autotune(kdgr_scene_t s, const kdgr_view* views, int n_views, int preci
     char line[256];
     snprintf(line, sizeof(line),
              "{\"schedule\": %d, \"min_blocks\": %d, \"chunk\": %d, \"precision\": %d, \"hit_buffer\": %d, "
-             "\"traversal\": %d, \"tile_shape\": %d, \"ms\": %.4f}\n",
-             c.schedule, c.min_blocks, c.chunk, c.precision, c.hit_buffer, c.traversal, c.tile_shape, med);
+             "\"traversal\": %d, \"tile_shape\": %d, \"rays_per_warp\": %d, \"ms\": %.4f}\n",
+             c.schedule, c.min_blocks, c.chunk, c.precision, c.hit_buffer, c.traversal, c.tile_shape,
+             c.rays_per_warp, med);
     rep += line;
     if (med < best_ms) {
       best_ms = med;

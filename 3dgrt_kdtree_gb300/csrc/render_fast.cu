@@ -26,11 +26,15 @@
 //   * warp packets (the default traversal): the 32 rays of a warp tile walk
 //     the tree together, each with its own interval and decisions, so a
 //     leaf's records are warp-uniform loads (pkt_trace below);
+//   * lane groups (16 or 8 rays per warp): 2 or 4 lanes hold each ray and
+//     split its leaves' candidate pairs, the group taking its hits in key
+//     order from the lanes' buffers -- shorter rays and more warps in flight
+//     for small batches, the same pixels bit for bit;
 //   * pixels are handed out in spatially coherent units (8x4 warp tiles,
 //     16x8 CTA blocks, or blocks / tiles from per-SM contiguous strips) so
 //     the rays sharing an SM's L1 are neighbours; the autotuner picks the
 //     schedule, the register cap (occupancy), the hit-buffer size, the
-//     traversal and the warp tile shape;
+//     traversal, the warp tile shape and the rays per warp;
 //   * precision form: FP16 rows of M with an FP32 mean and BF16 SH (32 + 96
 //     bytes per Gaussian instead of 48 + 192); Gaussians whose scale ratio
 //     exceeds 1e3 (or whose factors leave the FP16 range) read FP32 factors
@@ -433,10 +437,139 @@ __device__ __forceinline__ bool ray_init(const FastView& S, const CamInfo& C, in
   return (tmax >= tmin) & (tmax >= 0.f);
 }
 
+// ------------------------------------------------------------ lane groups
+// With fewer than 32 rays per warp, each ray is held by a group of LPR
+// consecutive lanes (LPR = 2 or 4).  The lanes of a group hold the same ray
+// state and take the same decisions; lane `sub` of the group tests pairs
+// sub, sub + LPR, ... of each leaf, and the group takes its hits in key
+// order from the lanes' buffers.  `mask` names the lanes that make the
+// collective calls together: the whole warp (packets) or the group
+// (independent rays).
+
+// Minimum over the group of the keys (t, i), carrying g.
+template <int LPR>
+__device__ __forceinline__ void group_min(float& t, uint32_t& i, float& g, unsigned mask) {
+#pragma unroll
+  for (int o = 1; o < LPR; o <<= 1) {
+    const float ot = __shfl_xor_sync(mask, t, o);
+    const uint32_t oi = __shfl_xor_sync(mask, i, o);
+    const float og = __shfl_xor_sync(mask, g, o);
+    if (ot < t || (ot == t && oi < i)) {
+      t = ot;
+      i = oi;
+      g = og;
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned group_mask(int LPR) {
+  const unsigned lane = threadIdx.x & 31u;
+  return ((1u << LPR) - 1u) << (lane & ~(unsigned)(LPR - 1));
+}
+
+// The candidate scan of one leaf pass for this lane's share of the pairs:
+// the K smallest (t, leaf position) keys above the last key taken, on
+// [tn, t_far).  Returns true when the share had more accepted hits than K.
+template <int K, bool PACKED, int LPR>
+__device__ __forceinline__ bool scan_share(const FastView& S, const LeafRef& L, const Ray& R, float tn,
+                                           unsigned mask, bool have_last, float last_t, uint32_t last_i,
+                                           HitBuf<K>& hb) {
+  const unsigned sub = threadIdx.x & (LPR - 1u);
+  bool overflow = false;
+  hb.clear();
+  const Ray2 w = ray2(R.o, R.d);
+  const uint32_t np = L.np + L.nf;
+  for (uint32_t pb = 0; pb < np; pb += LPR) {
+    const uint32_t p = pb + sub;
+    float t2[2], g2[2];
+    PairT pt;
+    // a lane past the end of the leaf tests its last pair again and drops it
+    unsigned m = leaf_pair_t<PACKED>(S, L, LPR == 1 || p < np ? p : np - 1u, w, tn, R.t_far, pt);
+    if (LPR > 1 && p >= np) m = 0u;
+    // uniform branches: most pairs have no lane with t* in range
+    if (__any_sync(mask, m != 0u)) {
+      m = test_pair_g(pt, m, t2, g2);
+      if (__any_sync(mask, m != 0u)) {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const uint32_t ik = 2 * p + k;
+          if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
+            overflow |= hb.insert(t2[k], g2[k], ik);
+        }
+      }
+    }
+  }
+  return overflow;
+}
+
+// Composite one accepted hit (t, g) of Gaussian gid: response, alpha with
+// the 0.99 cap, the 0.0113 / (1/255) skips, SH colour, front-to-back update.
+template <bool PACKED>
+__device__ __forceinline__ void blend_hit(const FastView& S, Ray& R, float t, float g, uint32_t gid) {
+  const float gres = __expf(-0.0555555555556f * g * g);
+  const float alpha = fminf(0.99f, gauss_opacity<PACKED>(S, gid) * gres);
+  if (gres < 0.0113f || alpha < 1.0f / 255.0f) return;
+  const F3 c = eval_sh_fast<PACKED>(S, gid, R.d);
+  const float w = alpha * (1.f - R.A);
+  R.r = fmaf(c.x, w, R.r);
+  R.g = fmaf(c.y, w, R.g);
+  R.b = fmaf(c.z, w, R.b);
+  R.D = fmaf(t, w, R.D);
+  R.A += w;
+}
+
+// The group takes its hits of one leaf pass in key order: the smallest
+// head key of the lanes' buffers, popped from the lane that holds it, as
+// long as no lane whose share overflowed has run out of buffered keys (its
+// next key is not known).  Every lane of the group blends the same hits.
+// Stops once A > 0.99.  Returns whether the group must re-scan the leaf
+// above (last_t, last_i).
+template <int K, bool PACKED, int LPR>
+__device__ __forceinline__ bool take_group_hits(const FastView& S, const LeafRef& L, Ray& R, const HitBuf<K>& hb,
+                                                bool overflow, unsigned mask, bool active, bool& ok,
+                                                float& last_t, uint32_t& last_i, uint32_t* status) {
+  const float kInf = __int_as_float(0x7f800000);
+  const unsigned gm = group_mask(LPR);
+  uint32_t h = 0;  // next unconsumed entry of this lane's buffer
+#pragma unroll 1
+  for (int it = 0; it < K * LPR; ++it) {
+    float kt = kInf, kg = 0.f;
+    uint32_t ki = 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (h == (uint32_t)k) {
+        kt = hb.t[k];
+        kg = hb.g[k];
+        ki = hb.i[k];
+      }
+    const bool blocked = (__ballot_sync(mask, overflow && h == (uint32_t)K) & gm) != 0u;
+    float mt = kt, mg = kg;
+    uint32_t mi = ki;
+    group_min<LPR>(mt, mi, mg, mask);
+    const bool act = active && ok && !blocked && mt != kInf && !(R.A > 0.99f);
+    if (!__any_sync(mask, act)) break;
+    if (act) {
+      if (kt == mt && ki == mi) ++h;
+      last_t = mt;
+      last_i = mi;
+      const uint32_t gid = leaf_gid<PACKED>(S, L, mi);
+      if (gid >= S.n_gauss) {
+        atomicOr(status, kStatusBadId);
+        ok = false;
+      } else {
+        blend_hit<PACKED>(S, R, mt, mg, gid);
+      }
+    }
+  }
+  return (__ballot_sync(mask, overflow) & gm) != 0u;
+}
+
 // Descend from R.cur to the next leaf, test and composite it, then pop or
 // restart (singlePassIntersectGaussian_sortNode_onlyShortStack,
-// cudaRenderer.cu:1552-1708).  Returns true when the ray is finished.
-template <int K, bool PACKED>
+// cudaRenderer.cu:1552-1708).  Returns true when the ray is finished.  With
+// LPR > 1 the lanes of a group walk the same ray together and split each
+// leaf's candidates.
+template <int K, bool PACKED, int LPR>
 __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kThreads], float (*s_t)[kThreads],
                                           int tid, Ray& R, uint32_t* status) {
   uint2 nd = __ldg(S.nodes + R.cur);
@@ -469,51 +602,55 @@ __device__ __forceinline__ bool leaf_step(const FastView& S, uint32_t (*s_id)[kT
   bool have_last = false;
   float last_t = 0.f;
   uint32_t last_i = 0;
-  while (true) {
-    HitBuf<K> hb;
-    hb.clear();
-    bool overflow = false;
-    {
-      const Ray2 w = ray2(R.o, R.d);
-      for (uint32_t p = 0; p < L.np + L.nf; ++p) {
-        float t2[2], g2[2];
-        PairT pt;
-        unsigned m = leaf_pair_t<PACKED>(S, L, p, w, R.t_near, R.t_far, pt);  // padding never passes
-        if (m) {
-          m = test_pair_g(pt, m, t2, g2);
+  if constexpr (LPR > 1) {
+    const unsigned gm = group_mask(LPR);
+    bool ok = true;
+    while (true) {
+      HitBuf<K> hb;
+      const bool overflow = scan_share<K, PACKED, LPR>(S, L, R, R.t_near, gm, have_last, last_t, last_i, hb);
+      const bool again = take_group_hits<K, PACKED, LPR>(S, L, R, hb, overflow, gm, true, ok, last_t, last_i, status);
+      if (!ok || R.A > 0.99f) return true;
+      if (!again) break;
+      have_last = true;
+    }
+  } else {
+    while (true) {
+      HitBuf<K> hb;
+      hb.clear();
+      bool overflow = false;
+      {
+        const Ray2 w = ray2(R.o, R.d);
+        for (uint32_t p = 0; p < L.np + L.nf; ++p) {
+          float t2[2], g2[2];
+          PairT pt;
+          unsigned m = leaf_pair_t<PACKED>(S, L, p, w, R.t_near, R.t_far, pt);  // padding never passes
+          if (m) {
+            m = test_pair_g(pt, m, t2, g2);
 #pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            const uint32_t ik = 2 * p + k;
-            if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
-              overflow |= hb.insert(t2[k], g2[k], ik);
+            for (int k = 0; k < 2; ++k) {
+              const uint32_t ik = 2 * p + k;
+              if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
+                overflow |= hb.insert(t2[k], g2[k], ik);
+            }
           }
         }
       }
-    }
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      if (hb.t[k] == __int_as_float(0x7f800000)) break;
-      const uint32_t gid = leaf_gid<PACKED>(S, L, hb.i[k]);
-      if (gid >= S.n_gauss) {
-        atomicOr(status, kStatusBadId);
-        return true;
+      for (int k = 0; k < K; ++k) {
+        if (hb.t[k] == __int_as_float(0x7f800000)) break;
+        const uint32_t gid = leaf_gid<PACKED>(S, L, hb.i[k]);
+        if (gid >= S.n_gauss) {
+          atomicOr(status, kStatusBadId);
+          return true;
+        }
+        blend_hit<PACKED>(S, R, hb.t[k], hb.g[k], gid);
+        if (R.A > 0.99f) return true;
       }
-      const float gres = __expf(-0.0555555555556f * hb.g[k] * hb.g[k]);
-      const float alpha = fminf(0.99f, gauss_opacity<PACKED>(S, gid) * gres);
-      if (gres < 0.0113f || alpha < 1.0f / 255.0f) continue;
-      const F3 c = eval_sh_fast<PACKED>(S, gid, R.d);
-      const float w = alpha * (1.f - R.A);
-      R.r = fmaf(c.x, w, R.r);
-      R.g = fmaf(c.y, w, R.g);
-      R.b = fmaf(c.z, w, R.b);
-      R.D = fmaf(hb.t[k], w, R.D);
-      R.A += w;
-      if (R.A > 0.99f) return true;
+      if (!overflow) break;
+      have_last = true;
+      last_t = hb.t[K - 1];
+      last_i = hb.i[K - 1];
     }
-    if (!overflow) break;
-    have_last = true;
-    last_t = hb.t[K - 1];
-    last_i = hb.i[K - 1];
   }
   if (R.t_far >= R.t_scene_far) return true;
   if (R.quant == 0) {
@@ -552,73 +689,51 @@ struct PktEnt {
 };
 
 // Leaf L for the lanes with part set; every lane runs the same candidate
-// loop (lanes without part test against an empty interval).  Inside the leaf
-// a ray stops compositing once A > 0.99.  Returns false on a bad Gaussian ID
-// (status set).
-template <int K, bool PACKED>
+// loop (lanes without part test against an empty interval).  With LPR > 1
+// the lanes of each group split the leaf's candidates and take the group's
+// hits in key order.  Inside the leaf a ray stops compositing once
+// A > 0.99.  Returns false on a bad Gaussian ID (status set).
+template <int K, bool PACKED, int LPR>
 __device__ __forceinline__ bool pkt_leaf(const FastView& S, const LeafRef& L, Ray& R, bool part,
                                          uint32_t* status) {
+  const unsigned full = 0xFFFFFFFFu;
   const float kInf = __int_as_float(0x7f800000);
   bool have_last = false, ok = true;
   float last_t = 0.f;
   uint32_t last_i = 0;
   bool more = part;
-  while (__any_sync(0xFFFFFFFFu, more)) {
+  while (__any_sync(full, more)) {
     HitBuf<K> hb;
-    hb.clear();
-    bool overflow = false;
-    const float tn = more ? R.t_near : kInf;
-    {
-      const Ray2 w = ray2(R.o, R.d);
-      for (uint32_t p = 0; p < L.np + L.nf; ++p) {
-        float t2[2], g2[2];
-        PairT pt;
-        unsigned m = leaf_pair_t<PACKED>(S, L, p, w, tn, R.t_far, pt);  // padding never passes
-        // warp-uniform branches: most pairs have no lane with t* in range
-        if (__any_sync(0xFFFFFFFFu, m != 0u)) {
-          m = test_pair_g(pt, m, t2, g2);
-          if (__any_sync(0xFFFFFFFFu, m != 0u)) {
+    const bool overflow =
+        scan_share<K, PACKED, LPR>(S, L, R, more ? R.t_near : kInf, full, have_last, last_t, last_i, hb);
+    if constexpr (LPR > 1) {
+      const bool again = take_group_hits<K, PACKED, LPR>(S, L, R, hb, overflow, full, more, ok, last_t, last_i,
+                                                         status);
+      more = more && ok && again && !(R.A > 0.99f);
+    } else {
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-              const uint32_t ik = 2 * p + k;
-              if (((m >> k) & 1u) && (!have_last || t2[k] > last_t || (t2[k] == last_t && ik > last_i)))
-                overflow |= hb.insert(t2[k], g2[k], ik);
-            }
-          }
+      for (int k = 0; k < K; ++k) {
+        if (hb.t[k] == kInf || R.A > 0.99f) break;
+        const uint32_t gid = leaf_gid<PACKED>(S, L, hb.i[k]);
+        if (gid >= S.n_gauss) {
+          atomicOr(status, kStatusBadId);
+          ok = false;
+          break;
         }
+        blend_hit<PACKED>(S, R, hb.t[k], hb.g[k], gid);
       }
+      more = more && ok && overflow && !(R.A > 0.99f);
+      last_t = hb.t[K - 1];
+      last_i = hb.i[K - 1];
     }
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      if (hb.t[k] == kInf || R.A > 0.99f) break;
-      const uint32_t gid = leaf_gid<PACKED>(S, L, hb.i[k]);
-      if (gid >= S.n_gauss) {
-        atomicOr(status, kStatusBadId);
-        ok = false;
-        break;
-      }
-      const float gres = __expf(-0.0555555555556f * hb.g[k] * hb.g[k]);
-      const float alpha = fminf(0.99f, gauss_opacity<PACKED>(S, gid) * gres);
-      if (gres < 0.0113f || alpha < 1.0f / 255.0f) continue;
-      const F3 c = eval_sh_fast<PACKED>(S, gid, R.d);
-      const float w = alpha * (1.f - R.A);
-      R.r = fmaf(c.x, w, R.r);
-      R.g = fmaf(c.y, w, R.g);
-      R.b = fmaf(c.z, w, R.b);
-      R.D = fmaf(hb.t[k], w, R.D);
-      R.A += w;
-    }
-    more = more && ok && overflow && !(R.A > 0.99f);
     have_last = true;
-    last_t = hb.t[K - 1];
-    last_i = hb.i[K - 1];
   }
   return ok;
 }
 
 // Trace the warp's rays as one packet.  live: the lane's ray entered the
 // scene box; sgn: bit a = sign of direction component a (warp-uniform).
-template <int K, bool PACKED>
+template <int K, bool PACKED, int LPR>
 __device__ __forceinline__ void pkt_trace(const FastView& S, Ray& R, bool live, unsigned sgn,
                                           uint32_t (*s_tn)[kThreads], float (*s_tf)[kThreads],
                                           PktEnt (*s_ent)[kWarps], int tid, int warp, uint32_t* status) {
@@ -668,7 +783,7 @@ __device__ __forceinline__ void pkt_trace(const FastView& S, Ray& R, bool live, 
       }
       const bool part = act && !done;
       if (__any_sync(full, part)) {
-        if (!pkt_leaf<K, PACKED>(S, L, R, part, status)) done = true;
+        if (!pkt_leaf<K, PACKED, LPR>(S, L, R, part, status)) done = true;
         if (part) {
           t_done = R.t_far;
           // inside a leaf only A > 0.99 stops a ray; at a leaf boundary the
@@ -733,9 +848,10 @@ __device__ __forceinline__ void store_px(const ViewDesc& V, int x, int y, const 
 }
 
 // Render the ray of pixel (x, y) of view V to completion and store it.
-// PKT: warp packets (every lane of the warp calls this together); otherwise
-// one independent ray per lane.
-template <int K, bool PACKED, bool PKT>
+// PKT: warp packets (every lane of the warp calls this together);
+// otherwise one independent ray per lane.  With LPR > 1 each group of LPR
+// consecutive lanes has the same pixel and its first lane stores it.
+template <int K, bool PACKED, bool PKT, int LPR>
 __device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, int x, int y,
                                           uint32_t (*s_id)[kThreads], float (*s_t)[kThreads],
                                           PktEnt (*s_ent)[kWarps], int tid, float* rgb, float* alpha_out,
@@ -754,17 +870,18 @@ __device__ __forceinline__ void render_px(const FastView& S, const ViewDesc& V, 
       const unsigned sgn = __shfl_sync(0xFFFFFFFFu, my_sgn, __ffs(pending) - 1);
       const bool in = live && my_sgn == sgn && ((pending >> (tid & 31)) & 1u);
       pending &= ~__ballot_sync(0xFFFFFFFFu, in);
-      pkt_trace<K, PACKED>(S, R, in, sgn, s_id, s_t, s_ent, tid, tid >> 5, status);
+      pkt_trace<K, PACKED, LPR>(S, R, in, sgn, s_id, s_t, s_ent, tid, tid >> 5, status);
     }
-    if (!inimg) return;
+    if (!inimg || (tid & (LPR - 1)) != 0) return;
     store_px(V, x, y, R, rgb, alpha_out, depth_out);
   } else {
     if (x >= W || y >= H) return;
     Ray R;
     if (ray_init(S, V.cam, x, y, R)) {
-      while (R.A < 0.99f && !leaf_step<K, PACKED>(S, s_id, s_t, tid, R, status)) {
+      while (R.A < 0.99f && !leaf_step<K, PACKED, LPR>(S, s_id, s_t, tid, R, status)) {
       }
     }
+    if ((tid & (LPR - 1)) != 0) return;
     store_px(V, x, y, R, rgb, alpha_out, depth_out);
   }
 }
@@ -785,6 +902,16 @@ __device__ __forceinline__ void block_pixel(int tile, int bx, int by, int q, int
   }
 }
 
+// Pixel of lane `lane` in item q (0 .. 4 LPR - 1) of the 16x8 block at
+// (bx, by) when LPR lanes share a ray: the block is cut into 4 x (8 / LPR)
+// tiles of 32 / LPR rays, 4 across and LPR down.
+template <int LPR>
+__device__ __forceinline__ void group_pixel(int bx, int by, int q, int lane, int& x, int& y) {
+  const int gi = lane / LPR;
+  x = bx + 4 * (q & 3) + (gi & 3);
+  y = by + (8 / LPR) * (q >> 2) + (gi >> 2);
+}
+
 // Persistent kernel.  Schedules (include/kdgr.h):
 //   WARP_TILES: each warp takes `chunk` 8x4 tiles from the global queue;
 //   WARP_STRIPS: each warp takes the next quarter of a 16x8 block of
@@ -794,7 +921,7 @@ __device__ __forceinline__ void block_pixel(int tile, int bx, int by, int q, int
 //               its four warps render the four quarters, so the rays sharing
 //               the SM's L1 are neighbours.
 // MINB caps registers so that MINB CTAs fit per SM (0: compiler's choice).
-template <bool PACKED, int SCHED, int MINB, int KB, bool PKT>
+template <bool PACKED, int SCHED, int MINB, int KB, bool PKT, int LPR>
 __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, const ViewDesc* __restrict__ views,
                                                                  int n_views, uint32_t total_items,
                                                                  float* __restrict__ rgb,
@@ -807,8 +934,9 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
   __shared__ uint32_t s_work;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if constexpr (SCHED == KDGR_SCHED_WARP_STRIPS) {
-    // items are quarters of 16x8 blocks (warp tiles in block order); each
-    // warp claims the next quarter of its SM's strip, no CTA barrier
+    // items are quarters of 16x8 blocks (warp tiles in block order), or with
+    // LPR lanes per ray 4 LPR tiles of 32 / LPR rays; each warp claims the
+    // next item of its SM's strip, no CTA barrier
     uint32_t smid;
     asm("mov.u32 %0, %%smid;" : "=r"(smid));
     const uint32_t n = (uint32_t)chunk;  // number of strips
@@ -823,12 +951,14 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
         ++visited;
         continue;
       }
-      const uint32_t blk = it >> 2, q = it & 3u;
+      const uint32_t blk = it / (4u * LPR), q = it % (4u * LPR);
       const ViewDesc& V = views[find_view(views, n_views, blk, KDGR_SCHED_CTA_BLOCKS)];
       const uint32_t lb = blk - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
       int x, y;
-      block_pixel(tile, (int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, (int)q, lane, x, y);
-      render_px<KB, PACKED, PKT>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
+      if constexpr (LPR == 1) block_pixel(tile, (int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, (int)q, lane, x, y);
+      else group_pixel<LPR>((int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, (int)q, lane, x, y);
+      render_px<KB, PACKED, PKT, LPR>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out,
+                                      status);
     }
   } else if constexpr (SCHED == KDGR_SCHED_SM_STRIPS) {
     // strip of this SM: [total * k / n, total * (k + 1) / n), k = smid mod n
@@ -857,7 +987,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
       const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
       int x, y;
       block_pixel(tile, (int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, warp, lane, x, y);
-      render_px<KB, PACKED, PKT>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
+      render_px<KB, PACKED, PKT, 1>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
     }
   } else {
     while (true) {
@@ -885,7 +1015,7 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
           x = (int)(lt % nx) * kTileW + (lane & 7);
           y = (int)(lt / nx) * kTileH + (lane >> 3);
         }
-        render_px<KB, PACKED, PKT>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
+        render_px<KB, PACKED, PKT, 1>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, alpha_out, depth_out, status);
       }
     }
   }
@@ -925,7 +1055,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_render_multi(const FastView* __
     const uint32_t lb = blk - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
     int x, y;
     block_pixel(KDGR_TILE_8X4, (int)(lb % nx) * kBlockW, (int)(lb / nx) * kBlockH, (int)(it & 3u), lane, x, y);
-    render_px<kHits, PACKED, true>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, nullptr, nullptr, status);
+    render_px<kHits, PACKED, true, 1>(S, V, x, y, s_id, s_t, s_ent, tid, rgb, nullptr, nullptr, status);
   }
 }
 
@@ -958,19 +1088,28 @@ __global__ void k_aniso_fp64(const float* __restrict__ src, uint32_t n, float4* 
 using KernelFn = void (*)(FastView, const ViewDesc*, int, uint32_t, float*, float*, float*, uint32_t*, uint32_t*,
                           int, int);
 
-template <bool PACKED, int SCHED, int KB, bool PKT>
+template <bool PACKED, int SCHED, int KB, bool PKT, int LPR>
 KernelFn pick_minb(int minb) {
-  if (minb >= 8) return k_render_batch<PACKED, SCHED, 8, KB, PKT>;
-  if (minb >= 6) return k_render_batch<PACKED, SCHED, 6, KB, PKT>;
-  return k_render_batch<PACKED, SCHED, 0, KB, PKT>;
+  if (minb >= 8) return k_render_batch<PACKED, SCHED, 8, KB, PKT, LPR>;
+  if (minb >= 6) return k_render_batch<PACKED, SCHED, 6, KB, PKT, LPR>;
+  return k_render_batch<PACKED, SCHED, 0, KB, PKT, LPR>;
+}
+
+// Lanes per ray: 32 / rays_per_warp (warp-strip schedule only).
+int lanes_per_ray(const kdgr_batch_config& c) {
+  return c.rays_per_warp == 8 ? 4 : c.rays_per_warp == 16 ? 2 : 1;
 }
 
 template <bool PACKED, int KB, bool PKT>
 KernelFn pick_sched_k(const kdgr_batch_config& c) {
-  if (c.schedule == KDGR_SCHED_CTA_BLOCKS) return pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS, KB, PKT>(c.min_blocks);
-  if (c.schedule == KDGR_SCHED_SM_STRIPS) return pick_minb<PACKED, KDGR_SCHED_SM_STRIPS, KB, PKT>(c.min_blocks);
-  if (c.schedule == KDGR_SCHED_WARP_STRIPS) return pick_minb<PACKED, KDGR_SCHED_WARP_STRIPS, KB, PKT>(c.min_blocks);
-  return pick_minb<PACKED, KDGR_SCHED_WARP_TILES, KB, PKT>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_CTA_BLOCKS) return pick_minb<PACKED, KDGR_SCHED_CTA_BLOCKS, KB, PKT, 1>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_SM_STRIPS) return pick_minb<PACKED, KDGR_SCHED_SM_STRIPS, KB, PKT, 1>(c.min_blocks);
+  if (c.schedule == KDGR_SCHED_WARP_STRIPS) {
+    if (lanes_per_ray(c) == 4) return pick_minb<PACKED, KDGR_SCHED_WARP_STRIPS, KB, PKT, 4>(c.min_blocks);
+    if (lanes_per_ray(c) == 2) return pick_minb<PACKED, KDGR_SCHED_WARP_STRIPS, KB, PKT, 2>(c.min_blocks);
+    return pick_minb<PACKED, KDGR_SCHED_WARP_STRIPS, KB, PKT, 1>(c.min_blocks);
+  }
+  return pick_minb<PACKED, KDGR_SCHED_WARP_TILES, KB, PKT, 1>(c.min_blocks);
 }
 
 template <bool PACKED, bool PKT>
@@ -1083,6 +1222,14 @@ int check_batch_config(kdgr_scene_t s, const kdgr_batch_config& c) {
     set_error("batch config: traversal must be KDGR_TRAV_PACKET or KDGR_TRAV_RAY");
     return KDGR_ERR_INVALID_ARG;
   }
+  if (c.rays_per_warp != 0 && c.rays_per_warp != 32 && c.rays_per_warp != 16 && c.rays_per_warp != 8) {
+    set_error("batch config: rays_per_warp must be 0, 32, 16 or 8");
+    return KDGR_ERR_INVALID_ARG;
+  }
+  if (lanes_per_ray(c) > 1 && (c.schedule != KDGR_SCHED_WARP_STRIPS || c.tile_shape != KDGR_TILE_8X4)) {
+    set_error("batch config: 16 or 8 rays per warp need the warp-strip schedule and the default tile shape");
+    return KDGR_ERR_INVALID_ARG;
+  }
   return KDGR_OK;
 }
 
@@ -1102,7 +1249,9 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
   const bool warp_strips = c.schedule == KDGR_SCHED_WARP_STRIPS;
   const bool per_warp = c.schedule == KDGR_SCHED_WARP_TILES || warp_strips;
   if (warp_strips && total_blocks > 0x3FFFFFFFu) return cudaErrorInvalidValue;
-  const uint32_t total = warp_strips ? 4u * total_blocks : per_warp ? total_tiles : total_blocks;
+  const uint32_t lpr = (uint32_t)lanes_per_ray(c);
+  if (warp_strips && total_blocks > 0x3FFFFFFFu / lpr) return cudaErrorInvalidValue;
+  const uint32_t total = warp_strips ? 4u * lpr * total_blocks : per_warp ? total_tiles : total_blocks;
   // SM strips: the kernel's `chunk` argument carries the number of strips
   const bool strips = c.schedule == KDGR_SCHED_SM_STRIPS || warp_strips;
   const int chunk = strips ? std::min(num_sms(), kMaxStrips) : c.chunk;

@@ -45,7 +45,7 @@ class View(ctypes.Structure):
 class BatchConfig(ctypes.Structure):
     _fields_ = [("schedule", ctypes.c_int32), ("min_blocks", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("chunk", ctypes.c_int32), ("precision", ctypes.c_int32), ("hit_buffer", ctypes.c_int32),
-                ("traversal", ctypes.c_int32), ("tile_shape", ctypes.c_int32)]
+                ("traversal", ctypes.c_int32), ("tile_shape", ctypes.c_int32), ("rays_per_warp", ctypes.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

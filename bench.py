@@ -214,7 +214,7 @@ def roofline(key: str, ms_step: float, clk: dict, sms: int, alg_bytes: float, ra
     out["memory"] = {
         "algorithmic_bytes_per_step": alg_bytes, "bytes_per_ray": round(alg_bytes / rays, 1),
         "algorithmic_gbs": round(alg_bytes / (ms_step * 1e-3) / 1e9, 1),
-        "note": "algorithmic bytes are L1/L2 demand: the frame's working set stays in the 126 MB L2",
+        "note": "algorithmic bytes are L1/L2 demand: the frame's working set stays in the 129 MB L2",
         "dram_bytes_per_launch": dram,
         "dram_gbs": round(dram / (ms_step * 1e-3) / 1e9, 2) if dram else None,
         "dram_frac_of_hbm": round(dram / (ms_step * 1e-3) / 1e9 / hbm, 5) if dram else None,

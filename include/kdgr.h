@@ -270,6 +270,9 @@ typedef struct {
                             accepted hits is re-scanned for the next ones */
   int32_t traversal;     /* KDGR_TRAV_*: how the rays of a warp walk the tree */
   int32_t tile_shape;    /* KDGR_TILE_*: the warp's pixel tile inside each 16x8 block */
+  int32_t rays_per_warp; /* 32 (0 = 32), 16 or 8: with fewer rays per warp, 2 or 4 lanes share each ray and
+                            split its leaves' candidate tests (more warps in flight and shorter rays for
+                            small batches); needs KDGR_SCHED_WARP_STRIPS, warp packets and 8x4 tiles */
 } kdgr_batch_config;
 
 void kdgr_batch_config_default(kdgr_batch_config* cfg);

@@ -100,13 +100,39 @@ def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
                                                (2, 1, 0, 8, 1, 0), (2, 1, 8, 4, 0, 2), (1, 1, 8, 4, 1, 1),
                                                (2, 1, 8, 8, 1, 1), (3, 1, 8, 4, 0, 0), (3, 1, 0, 8, 1, 2),
                                                (3, 1, 6, 4, 0, 1)]:
-        cfg = F.BatchConfig(sched, minb, 0, chunk, 0, kb, trav, tile)
+        cfg = F.BatchConfig(sched, minb, 0, chunk, 0, kb, trav, tile, 32)
         out = torch.full_like(ref, -1.0)
         out_a = torch.full_like(ref_a, -1.0)
         scene.render_batch(views, len(cams), out, out_a, cfg=cfg)
         torch.cuda.synchronize()
         assert float((out - ref).abs().max()) <= 1e-5, (sched, chunk, minb, trav, tile)
         assert float((out_a - ref_a).abs().max()) <= 1e-5, (sched, chunk, minb, trav, tile)
+    scene.close()
+
+
+@pytest.mark.parametrize("name", ["cluster2k", "dense800", "uniform2k"])
+def test_rays_per_warp_renders_the_same_pixels(pkg, cuda, fixtures, name):
+    """16 or 8 rays per warp (2 or 4 lanes sharing each ray, each testing
+    every 2nd or 4th candidate pair, hits merged in key order across the
+    lanes) composite exactly the hits of 32 rays per warp in the same order:
+    the pixels, alpha and depth are bit-identical, for both forms, both
+    traversals, both hit buffer sizes and every register cap."""
+    fx = fixtures[name]
+    F = pkg.renderer
+    scene = F.Scene(fx.tree, fx.rec, forms=F.FORM_FAST | F.FORM_PACKED)
+    cams = pkg.scenes.sphere_cameras(5, seed=13, resolutions=[(67, 41), (96, 64), (8, 3)])
+    views, total, _ = F.make_views(cams)
+    for prec in (0, 1):
+        ref = [torch.zeros(total * 3, device=cuda), torch.zeros(total, device=cuda), torch.zeros(total, device=cuda)]
+        scene.render_batch(views, len(cams), *ref, cfg=F.BatchConfig(3, 8, 0, 1, prec, 4, 0, 0, 32))
+        for rpw, minb, kb, trav in [(16, 8, 4, 0), (8, 8, 4, 0), (16, 0, 8, 0), (8, 6, 8, 0), (16, 8, 4, 1),
+                                    (8, 8, 4, 1), (8, 0, 8, 1)]:
+            out = [torch.full_like(t, -1.0) for t in ref]
+            scene.render_batch(views, len(cams), *out, cfg=F.BatchConfig(3, minb, 0, 1, prec, kb, trav, 0, rpw))
+            torch.cuda.synchronize()
+            for a, b in zip(out, ref):
+                np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+    assert scene.status() == 0
     scene.close()
 
 
@@ -119,11 +145,12 @@ def test_autotune_picks_a_valid_config(pkg, cuda, fixtures):
     rgb = torch.zeros(total * 3, device=cuda)
     best, report = scene.autotune(views, len(cams), rgb)
     assert best.schedule in (0, 1, 2, 3) and best.chunk in (1, 2) and best.min_blocks in (0, 6, 8)
-    # 18 stage-1 lines, then 8-entry buffer, per-ray traversal and (unless the
-    # warp-tile schedule won stage 1) the 4x8 and 16x2 tile shapes
-    assert len(report.strip().splitlines()) in (20, 22)
+    # 18 stage-1 lines, then 8-entry buffer, per-ray traversal, (unless the
+    # warp-tile schedule won stage 1) the 4x8 and 16x2 tile shapes, and 16 and
+    # 8 rays per warp with either traversal
+    assert len(report.strip().splitlines()) in (24, 26)
     assert best.hit_buffer in (4, 8) and best.traversal in (F.TRAV_PACKET, F.TRAV_RAY)
-    assert best.tile_shape in (F.TILE_8X4, F.TILE_4X8, F.TILE_16X2)
+    assert best.tile_shape in (F.TILE_8X4, F.TILE_4X8, F.TILE_16X2) and best.rays_per_warp in (32, 16, 8)
     ref = torch.zeros_like(rgb)
     scene.render_batch(views, len(cams), ref)
     out = torch.zeros_like(rgb)
@@ -144,7 +171,10 @@ def test_batch_config_errors(pkg, cuda, fixtures):
     scene.close()
     scene = F.Scene(fx.tree, fx.rec)
     for bad in (F.BatchConfig(0, 8, 0, 1, 0, 4, 0, F.TILE_4X8),  # warp tiles are 8x4 only
-                F.BatchConfig(1, 8, 0, 1, 0, 4, 0, 7), F.BatchConfig(1, 8, 0, 1, 0, 4, 5, 0)):
+                F.BatchConfig(1, 8, 0, 1, 0, 4, 0, 7), F.BatchConfig(1, 8, 0, 1, 0, 4, 5, 0),
+                F.BatchConfig(3, 8, 0, 1, 0, 4, 0, 0, 12),  # 32, 16 or 8 rays per warp
+                F.BatchConfig(1, 8, 0, 1, 0, 4, 0, 0, 16),  # fewer rays per warp need warp strips
+                F.BatchConfig(3, 8, 0, 1, 0, 4, 1, 2, 8)):  # ... and 8x4 tiles
         with pytest.raises(pkg.capi.KdgrError):
             scene.render_batch(views, 1, rgb, cfg=bad)
     scene.close()
@@ -170,7 +200,7 @@ def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
     a split, an empty scene, a missed box, and leaves mixing very thin
     Gaussians (the precision form's FP32 stream) with plain ones; both forms
     within the accuracy bar of the FP64 oracle and equal across every
-    schedule, tile shape and both traversals."""
+    schedule, tile shape, both traversals and 32, 16 or 8 rays per warp."""
     import kat
     (tree, rec, cam), W, H = KAT_CASES[case](kat)
     F = pkg.renderer
@@ -186,10 +216,11 @@ def test_fast_forms_on_known_answer_scenes(pkg, O, cuda, case):
     for prec in (0, 1):
         ref = torch.zeros(total * 3, device=cuda)
         scene.render_batch(views, 1, ref, cfg=F.BatchConfig(1, 8, 0, 1, prec, 4, 0, 0))
-        for sched, kb, trav, tile in [(0, 4, 0, 0), (1, 8, 0, 1), (2, 4, 0, 2), (3, 4, 0, 1), (0, 4, 1, 0),
-                                      (1, 8, 1, 2), (3, 8, 1, 0)]:
+        for sched, kb, trav, tile, rpw in [(0, 4, 0, 0, 32), (1, 8, 0, 1, 32), (2, 4, 0, 2, 32), (3, 4, 0, 1, 32),
+                                           (0, 4, 1, 0, 32), (1, 8, 1, 2, 32), (3, 8, 1, 0, 32), (3, 4, 0, 0, 16),
+                                           (3, 8, 0, 0, 8), (3, 4, 0, 0, 8), (3, 4, 1, 0, 16), (3, 8, 1, 0, 8)]:
             out = torch.full_like(ref, -1.0)
-            scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, prec, kb, trav, tile))
+            scene.render_batch(views, 1, out, cfg=F.BatchConfig(sched, 8, 0, 1, prec, kb, trav, tile, rpw))
             torch.cuda.synchronize()
             np.testing.assert_array_equal(out.cpu().numpy(), ref.cpu().numpy())
     assert scene.status() == 0
