@@ -7,8 +7,8 @@
 //   * arithmetic: FMA, fast reciprocal, __expf; the ray-Gaussian test reads
 //     the precomputed rows of M = diag(1/s) R^T (with b = M mu folded in for
 //     the FP32 form), forms ng = M (mu - o) and grdu = M d, accepts t* on
-//     the leaf interval without a reciprocal and only then evaluates the
-//     Mahalanobis distance;
+//     the leaf interval without a reciprocal (by the signs of two fused
+//     multiply-adds) and only then evaluates the Mahalanobis distance;
 //   * hits are accepted with t* in the half-open interval [t_near, t_far),
 //     so a Gaussian straddling a split plane is composited in one leaf only;
 //   * the tree is relaid out with its top levels breadth-first (they stay
@@ -184,8 +184,13 @@ struct PairT {
 __device__ __forceinline__ unsigned pair_t(PairT& p, float t_near, float t_far) {
   const f2 q = fma2(p.gd[0], p.gd[0], fma2(p.gd[1], p.gd[1], mul2(p.gd[2], p.gd[2])));
   const f2 a = fma2(p.gd[0], p.ng[0], fma2(p.gd[1], p.ng[1], mul2(p.gd[2], p.ng[2])));
-  // t* = a / q in [t_near, t_far)  <=>  a in [t_near q, t_far q)  (q > 0)
-  const f2 lo = mul2(q, bcast2(t_near)), hi = mul2(q, bcast2(t_far));
+  // t* = a / q in [t_near, t_far)  <=>  a - t_near q >= 0 and a - t_far q < 0  (q > 0),
+  // each difference formed by one fused multiply-add and read by its sign.
+  // A leaf's t_far is the next leaf's t_near, so one rounded difference
+  // decides both sides of a split plane: a Gaussian straddling it is
+  // accepted in exactly one of the two leaves.  Padding entries (q = a = 0)
+  // give +0 on both sides and are refused.
+  const f2 lo = fma2(q, bcast2(-t_near), a), hi = fma2(q, bcast2(-t_far), a);
   float q0, q1, a0, a1, l0, l1, h0, h1;
   split2(q, q0, q1);
   split2(a, a0, a1);
@@ -195,7 +200,8 @@ __device__ __forceinline__ unsigned pair_t(PairT& p, float t_near, float t_far) 
   p.q1 = q1;
   p.a0 = a0;
   p.a1 = a1;
-  return ((a0 >= l0 && a0 < h0) ? 1u : 0u) | ((a1 >= l1 && a1 < h1) ? 2u : 0u);
+  const uint32_t m0 = __float_as_uint(h0) & ~__float_as_uint(l0), m1 = __float_as_uint(h1) & ~__float_as_uint(l1);
+  return (m0 >> 31) | ((m1 >> 31) << 1);
 }
 // FP32 pair: ng = b - M o.
 __device__ __forceinline__ void setup_pair(const PairRec& r, const Ray2& w, PairT& p) {
@@ -362,13 +368,10 @@ template <int K>
 struct HitBuf {
   float t[K], g[K];
   uint32_t i[K];
+  // only t: g and i are read where t is finite, and insert moves them with t
   __device__ __forceinline__ void clear() {
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      t[k] = __int_as_float(0x7f800000);
-      g[k] = 0.f;
-      i[k] = 0u;
-    }
+    for (int k = 0; k < K; ++k) t[k] = __int_as_float(0x7f800000);
   }
   // returns true when an entry fell off the end (the leaf needs another pass)
   __device__ __forceinline__ bool insert(float ct, float cg, uint32_t ci) {
