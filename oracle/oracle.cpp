@@ -14,7 +14,6 @@
 #include <vector>
 
 #include "oracle.h"
-#include "kdgr_math.h"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -67,7 +66,34 @@ inline V3<R> safe_normalize(V3<R> v) {
   return l > R(0) ? muls(v, R(1) / std::sqrt(l)) : v;
 }
 
-inline float rexp(float x) { return kdgr_expf(x); }
+// The exponential of the oracle-matching arithmetic.  The reference calls
+// CUDA's expf in particleResponse (cudaRenderer.cu:676-680); a CPU
+// restatement cannot reproduce a vendor-library result, so the oracle and
+// the plain kernel both use one published method instead, each in its own
+// code: Cody-Waite reduction x = k ln2 + r with ln2 split into C1 = 355/512
+// (9 significant bits, so k*C1 is exact) and C2 = ln2 - C1 (W. J. Cody and
+// W. Waite, "Software Manual for the Elementary Functions", 1980), then
+// e^r by its Taylor series to degree 7 in Horner form, scaled by 2^k.  In
+// FP32 round-to-nearest without contraction, in this order, the two give
+// the same bits; tests/test_oracle.py checks that on a dense sample of the
+// response domain and bounds the error against double-precision exp.
+inline float oracle_expf(float x) {
+  if (!(x >= -87.3f)) return (x != x) ? x : 0.0f;
+  if (x > 88.0f) return HUGE_VALF;
+  const float k = std::floor(x * 1.44269504088896341f + 0.5f);  // round(x / ln2)
+  float r = x - k * 0.693359375f;                               // C1 = 355/512
+  r = r + k * 2.12194440e-4f;                                    // -C2
+  static const float kTaylor[8] = {1.0f / 5040, 1.0f / 720, 1.0f / 120, 1.0f / 24,
+                                   1.0f / 6,    0.5f,       1.0f,       1.0f};
+  float p = kTaylor[0];
+  for (int i = 1; i < 8; ++i) p = p * r + kTaylor[i];
+  const uint32_t bits = (uint32_t)((int)k + 127) << 23;
+  float scale;
+  std::memcpy(&scale, &bits, 4);
+  return p * scale;
+}
+
+inline float rexp(float x) { return oracle_expf(x); }
 inline double rexp(double x) { return std::exp(x); }
 
 // quaternionWXYZToMatrixTranspose (cudaRenderer.cu:808-828).
@@ -574,6 +600,10 @@ int orc_render_f64(const orc_scene* s, const orc_caminfo* c, int width, int heig
   return render<double>(s, c, width, height, pix, n_pix, rgb, alpha, depth, trace, threads);
 }
 
-float orc_expf(float x) { return kdgr_expf(x); }
+float orc_expf(float x) { return oracle_expf(x); }
+
+void orc_expf_n(const float* x, float* y, uint32_t n) {
+  for (uint32_t i = 0; i < n; ++i) y[i] = oracle_expf(x[i]);
+}
 
 }  // extern "C"

@@ -71,6 +71,8 @@ int orc_render_hybrid_f32(const orc_scene* s, const orc_caminfo* c, int width, i
 
 /* kdgr_expf, exported for the error test. */
 float orc_expf(float x);
+/* The same over an array. */
+void orc_expf_n(const float* x, float* y, uint32_t n);
 
 #ifdef __cplusplus
 }

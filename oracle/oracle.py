@@ -24,8 +24,7 @@ def build(cxx: str = "g++") -> str:
     """Compile liboracle with the flags the transcription requires."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-           "-I" + os.path.join(REPO, "include"), "-I" + os.path.join(REPO, "3dgrt_kdtree_gb300", "csrc"),
-           os.path.join(HERE, "oracle.cpp"), "-o", LIB]
+           "-I" + os.path.join(REPO, "include"), os.path.join(HERE, "oracle.cpp"), "-o", LIB]
     subprocess.run(cmd, check=True)
     return LIB
 
@@ -69,6 +68,8 @@ def lib() -> ctypes.CDLL:
                                             ctypes.c_uint32, vp, vp, ctypes.c_int]
         L.orc_expf.argtypes = [ctypes.c_float]
         L.orc_expf.restype = ctypes.c_float
+        L.orc_expf_n.argtypes = [vp, vp, ctypes.c_uint32]
+        L.orc_expf_n.restype = None
         _lib = L
     return _lib
 

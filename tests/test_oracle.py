@@ -1,5 +1,7 @@
 """The CPU oracle, pinned: golden outputs, known-answer scenes, the project
 exponential.  CPU only."""
+import os
+
 import numpy as np
 import pytest
 
@@ -21,8 +23,9 @@ def oscene(O, tree, rec):
 
 
 def test_expf_error_bound(O):
-    """kdgr_expf against double exp: <= 2 ulp on [-87, 0], and the relative
-    error on the response domain [-3.6, 0] stays below 2.5e-7."""
+    """The oracle's exponential against double exp: <= 2 ulp on [-87, 0],
+    and the relative error on the response domain [-3.6, 0] stays below
+    2.5e-7."""
     xs = np.linspace(-87.0, 0.0, 200_001, dtype=np.float32)
     got = np.array([O.lib().orc_expf(float(x)) for x in xs[::7]], np.float32)
     ref = np.exp(xs[::7].astype(np.float64))
@@ -34,6 +37,33 @@ def test_expf_error_bound(O):
     assert rel.max() < 2.5e-7, rel.max()
     assert O.lib().orc_expf(0.0) == 1.0
     assert O.lib().orc_expf(-100.0) == 0.0
+
+
+def test_oracle_expf_equals_the_kernels(O, tmp_path):
+    """The oracle restates the project exponential in its own code; the plain
+    kernel calls the product's (3dgrt_kdtree_gb300/csrc/kdgr_math.h).  Both
+    give the same bits: every float of the response domain's tail below
+    -3.6 at a stride, all floats in [-3.6, 0] at a finer stride, and the
+    edges of the domain."""
+    import ctypes
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    so = str(tmp_path / "probe.so")
+    subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-shared", "-fPIC",
+                    "-I" + os.path.join(os.path.dirname(here), "3dgrt_kdtree_gb300", "csrc"),
+                    os.path.join(here, "cpp", "expf_probe.c"), "-o", so, "-lm"], check=True)
+    probe = ctypes.CDLL(so)
+    lo = np.float32(-3.6).view(np.uint32)  # negative floats: bits grow with magnitude
+    dense = np.arange(0x80000000, lo, 97, dtype=np.uint32).view(np.float32)
+    tail = np.arange(lo, np.float32(-87.3).view(np.uint32), 1009, dtype=np.uint32).view(np.float32)
+    edges = np.array([0.0, -0.0, -87.29, -87.3, -87.31, -100.0, 1.0, 10.0, 88.0, 88.5, np.nan], np.float32)
+    xs = np.ascontiguousarray(np.concatenate([dense, tail, edges]))
+    a = np.empty_like(xs)
+    b = np.empty_like(xs)
+    O.lib().orc_expf_n(xs.ctypes.data, a.ctypes.data, xs.size)
+    probe.probe_expf_n(ctypes.c_void_p(xs.ctypes.data), ctypes.c_void_p(b.ctypes.data), ctypes.c_uint32(xs.size))
+    assert xs.size > 2_000_000
+    np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
 @pytest.mark.parametrize("name", ["uniform2k", "cluster2k", "dense800"])
