@@ -1,10 +1,11 @@
-/* kdgr_math.h -- arithmetic shared bit-for-bit by the device kernels and the
- * CPU oracle (C, compiled with -ffp-contract=off).
+/* kdgr_math.h -- the exponential of the oracle-matching kernels (C; on the
+ * host compiled with -ffp-contract=off).
  *
  * The reference kernel uses CUDA's expf inside particleResponse
  * (cudaRenderer.cu:663-680).  A CPU restatement cannot reproduce a
- * vendor-library result bit for bit, so the oracle-matching build uses this
- * project exponential on both sides instead:
+ * vendor-library result bit for bit, so the oracle-matching kernels use this
+ * project exponential instead, and the CPU oracle restates the same method
+ * in its own code (the two agree bit for bit):
  *
  *   exp(x) = 2^k * e^r,  k = floor(x*log2(e) + 1/2),
  *   r = (x - k*C1) - k*C2  with C1 = 355/512 and C2 = ln2 - C1
@@ -13,8 +14,9 @@
  *   e^r from its Taylor series to degree 7 by Horner's rule.
  *
  * On |r| <= ln2/2 the series truncation is below r^8/8! < 6e-9 relative
- * (0.1 ulp); the measured maximum error against a double-precision exp over
- * the response domain is checked by tests/test_oracle.py.  Domain: x <= 88
+ * (0.1 ulp); the maximum error against a double-precision exp over the
+ * response domain, and the agreement with the oracle's copy, are checked by
+ * tests/test_oracle.py.  Domain: x <= 88
  * (the renderer only evaluates x <= 0); x < -87.3 returns 0.
  *
  * KDGR_MUL/KDGR_ADD are IEEE round-to-nearest operations that the CUDA
