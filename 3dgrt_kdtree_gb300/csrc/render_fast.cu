@@ -45,6 +45,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <cfloat>
 #include <cstdint>
 #include <cstring>
@@ -1145,6 +1146,37 @@ int num_sms() {
   return n;
 }
 
+// Resident 128-thread CTAs per SM of a kernel on the current device (at
+// least 1), cached per kernel and device: the query costs microseconds and
+// every batched launch needs it.
+cudaError_t resident_ctas(const void* fn, int* out) {
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<const void*, int>, int>> cache;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (const auto& it : cache)
+      if (it.first.first == fn && it.first.second == dev) {
+        *out = it.second;
+        return cudaSuccess;
+      }
+  }
+  int occ = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  occ = occ > 0 ? occ : 1;
+  std::lock_guard<std::mutex> lk(mu);
+  cache.push_back({{fn, dev}, occ});
+  *out = occ;
+  return cudaSuccess;
+}
+template <typename F>
+cudaError_t resident_ctas(F* fn, int* out) {
+  return resident_ctas(reinterpret_cast<const void*>(fn), out);
+}
+
 }  // namespace
 
 // Host: view table and total tile count for a list of views.
@@ -1244,10 +1276,8 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
   KernelFn fn = pick_kernel(c);
   int per_sm = c.blocks_per_sm;
   if (per_sm <= 0) {
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreads, 0);
+    cudaError_t e = resident_ctas(fn, &per_sm);
     if (e != cudaSuccess) return e;
-    per_sm = occ > 0 ? occ : 1;
   }
   const bool warp_strips = c.schedule == KDGR_SCHED_WARP_STRIPS;
   const bool per_warp = c.schedule == KDGR_SCHED_WARP_TILES || warp_strips;
@@ -1442,7 +1472,7 @@ cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* 
                          uint32_t total_blocks, float* rgb, uint32_t* queue, uint32_t* status, cudaStream_t st) {
   auto fn = packed ? k_render_multi<true> : k_render_multi<false>;
   int occ = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreads, 0);
+  cudaError_t e = resident_ctas(reinterpret_cast<const void*>(fn), &occ);
   if (e != cudaSuccess) return e;
   if (total_blocks > 0x3FFFFFFFu) return cudaErrorInvalidValue;
   const uint32_t quarters = 4u * total_blocks;

@@ -147,10 +147,13 @@ capi._EXTRA_SIGS.update({
 
 
 def _ptr(t) -> Optional[int]:
+    """Address of a contiguous CUDA tensor, or of a contiguous pinned CPU
+    tensor (page-locked host memory is addressable from the device at the
+    same address, so a kernel can write its output straight into it)."""
     if t is None:
         return None
-    if not t.is_cuda or not t.is_contiguous():
-        raise ValueError("device buffers must be contiguous CUDA tensors")
+    if not t.is_contiguous() or not (t.is_cuda or t.is_pinned()):
+        raise ValueError("buffers must be contiguous CUDA tensors or pinned host tensors")
     return t.data_ptr()
 
 

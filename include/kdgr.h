@@ -11,6 +11,9 @@
  *     kdgr_last_error() gives the message of the calling thread's last error;
  *   - plain pointers and sizes; device buffers are raw CUDA device pointers,
  *     streams are cudaStream_t passed as void*; the caller owns every buffer;
+ *     render outputs may also be page-locked host memory (cudaHostAlloc /
+ *     cudaMallocHost), which the kernels then write directly -- on GB300 over
+ *     NVLink-C2C while the frame renders, with no separate copy;
  *   - a scene handle may be used from several threads; calls on one handle
  *     that write the same output buffers must be ordered by the caller;
  *   - every call on a scene runs on the device the scene was created on

@@ -82,6 +82,27 @@ def test_batch_equals_single_views_and_graph(pkg, cuda, fixtures):
     scene.close()
 
 
+def test_batch_output_in_pinned_host_memory(pkg, cuda, fixtures):
+    """Output buffers may be pinned host memory: the kernel writes the frame
+    straight into it, bit-identical to a device buffer."""
+    fx = fixtures["cluster2k"]
+    F = pkg.renderer
+    scene = F.Scene(fx.tree, fx.rec)
+    cams = pkg.scenes.sphere_cameras(3, seed=14, resolutions=[(64, 48), (17, 9)])
+    views, total, _ = F.make_views(cams)
+    dev_rgb = torch.zeros(total * 3, device=cuda)
+    dev_a = torch.zeros(total, device=cuda)
+    scene.render_batch(views, len(cams), dev_rgb, dev_a)
+    host_rgb = torch.full((total * 3,), -1.0).pin_memory()
+    host_a = torch.full((total,), -1.0).pin_memory()
+    scene.render_batch(views, len(cams), host_rgb, host_a)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(host_rgb.numpy(), dev_rgb.cpu().numpy())
+    np.testing.assert_array_equal(host_a.numpy(), dev_a.cpu().numpy())
+    assert scene.status() == 0
+    scene.close()
+
+
 def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     """Warp tiles, CTA blocks, SM strips and warp strips (with several chunk sizes and
     register caps) only change which lane renders which pixel; warp packets
