@@ -111,3 +111,39 @@ def test_scene_from_files_renders_as_host_upload(pkg, O, cuda, tmp_path):
     np.testing.assert_allclose(outs[1][0].reshape(H, W, 3), O.to_image(r32, W, H), rtol=0, atol=1e-5)
     for s in (a, b, c):
         s.close()
+
+
+def test_device_ingest_errors(pkg, cuda, tmp_path):
+    """Missing files, a tree whose IDs exceed the PLY's vertices, inverted
+    scales (PLY records are activated) and a buffer too small for the file
+    are refused with the library's status codes; nothing is left half made."""
+    sc = pkg.scenes
+    F = pkg.renderer
+    KdgrError = pkg.capi.KdgrError
+    ply = str(tmp_path / "a.ply")
+    sc.write_ply(ply, sc.raw_gaussians(500, seed=3))
+    rec = pkg.kdtree.read_ply(ply)
+    tree = pkg.kdtree.build(rec)
+    kdt = str(tmp_path / "a.kdt")
+    pkg.kdtree.write_kdt(tree, kdt)
+    small = str(tmp_path / "small.ply")
+    sc.write_ply(small, sc.raw_gaussians(100, seed=4))
+    cases = [((str(tmp_path / "missing.ply"), kdt, F.FORM_FAST), 4),   # KDGR_ERR_IO
+             ((ply, str(tmp_path / "missing.kdt"), F.FORM_FAST), 4),
+             ((small, kdt, F.FORM_FAST), 5),                            # IDs >= 100: KDGR_ERR_FORMAT
+             ((ply, kdt, F.FORM_FAST | F.SCALES_INVERTED), 1)]          # KDGR_ERR_INVALID_ARG
+    for args, status in cases:
+        with pytest.raises(KdgrError) as ei:
+            F.Scene.from_files(*args)
+        assert f"status {status}" in str(ei.value), (args, str(ei.value))
+    # a device buffer smaller than the file: KDGR_ERR_LIMIT
+    import ctypes
+    buf = torch.zeros((499, 64), device=cuda)
+    n = ctypes.c_uint32()
+    L = pkg.capi.lib()
+    rc = L.kdgr_read_ply_device(ply.encode(), ctypes.c_void_p(buf.data_ptr()), 499, ctypes.byref(n), None)
+    assert rc == 10 and b"capacity" in L.kdgr_last_error()
+    # the good pair still works after the failures
+    s = F.Scene.from_files(ply, kdt, forms=F.FORM_FAST)
+    assert s.info()["n_gaussians"] == 500
+    s.close()
