@@ -10,13 +10,16 @@
 //     submit and queued; the scheduler thread admits requests in arrival
 //     order while their output fits in the arena, and launches everything
 //     admitted as ONE persistent multi-scene launch on a free lane (stream);
+//     a request whose buffer is page-locked host memory takes no arena
+//     space: the kernel writes its frames straight into the buffer (each
+//     view of a launch carries its own output base);
 //     with several lanes, requests that arrive while a launch runs are
 //     admitted into the next lane's launch, so their work overlaps on the
 //     device (continuous batching: no fixed tick, a lane launches as soon as
 //     it is free and work is queued);
-//   * the completion thread waits for launches in launch order, copies each
-//     request's frames to its host buffer, frees the arena range and wakes
-//     waiters; latency = completion - submit;
+//   * the completion thread waits for launches in launch order, copies the
+//     frames of each arena request to its host buffer, frees the arena range
+//     and wakes waiters; latency = completion - submit;
 //   * every ray depends only on its own view, so a request's frames are the
 //     same alone and in any mix (tests/test_serving.py checks bit equality).
 // Waits on the host are bounded (kdgr_server_wait takes a timeout); the
@@ -45,6 +48,9 @@ using Clock = std::chrono::steady_clock;
 namespace {
 
 constexpr int kMaxSlots = 64;
+// launch-table bytes per view: its ViewDesc and its output base
+constexpr size_t kTableEntry = sizeof(ViewDesc) + sizeof(float*);
+static_assert(sizeof(ViewDesc) % alignof(float*) == 0, "output bases follow the views");
 
 // First-fit allocator over the output arena (units: RGB pixels).
 struct Arena {
@@ -93,7 +99,9 @@ struct Request {
   std::vector<kdgr_view> views;  // out_offset relative to the request
   uint64_t pixels = 0, rays = 0;
   float* host_rgb = nullptr;
-  size_t dev_off = 0;  // first pixel of the request in the arena
+  bool direct = false;      // page-locked host_rgb: the kernel writes it, no arena range
+  float* out_dev = nullptr; // host_rgb's device address when direct
+  size_t dev_off = 0;       // first pixel of the request in the arena
   ReqState state = kQueued;
   int status = KDGR_OK;
   bool cancel = false;
@@ -103,8 +111,9 @@ struct Request {
 struct Lane {
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
+  // launch table: k views, then k output bases (float*); h_views is pinned
   ViewDesc* d_views = nullptr;
-  ViewDesc* h_views = nullptr;  // pinned
+  ViewDesc* h_views = nullptr;
   uint32_t* d_queue = nullptr;
   bool busy = false;
   std::vector<Request*> reqs;
@@ -183,7 +192,7 @@ void kdgr_server_s::scheduler() {
       }
       if (!admitted.empty() && nv + r->views.size() > (size_t)cfg.max_views_per_launch) break;
       size_t off = 0;
-      if (!arena.alloc(r->pixels, &off)) break;  // arrival order: wait for space
+      if (!r->direct && !arena.alloc(r->pixels, &off)) break;  // arrival order: wait for space
       queue.pop_front();
       r->dev_off = off;
       r->state = kRunning;
@@ -195,11 +204,16 @@ void kdgr_server_s::scheduler() {
       cv_sched.wait_for(lk, std::chrono::milliseconds(50));
       continue;
     }
-    // view table: every view of every admitted request, blocks numbered in order
+    // view table: every view of every admitted request, blocks numbered in
+    // order; output bases follow the views
+    size_t nt = 0;
+    for (Request* r : admitted) nt += r->views.size();
+    float** h_outs = reinterpret_cast<float**>(L.h_views + nt);
     uint64_t cbase = 0;
     size_t k = 0;
     for (Request* r : admitted) {
       for (const kdgr_view& v : r->views) {
+        h_outs[k] = r->direct ? r->out_dev : d_arena;
         ViewDesc& d = L.h_views[k++];
         d.cam = make_caminfo(v.cam, v.width, v.height);
         d.W = v.width;
@@ -208,7 +222,7 @@ void kdgr_server_s::scheduler() {
         d.wt_base = 0;
         d.cb_x = (uint32_t)((v.width + 15) / 16);
         d.cb_base = (uint32_t)cbase;
-        d.out_off = r->dev_off + v.out_offset;
+        d.out_off = (r->direct ? 0 : r->dev_off) + v.out_offset;
         d.scene = (uint32_t)r->slot;
         d.pad = 0;
         cbase += (uint64_t)d.cb_x * (uint64_t)((v.height + 7) / 8);
@@ -224,10 +238,11 @@ void kdgr_server_s::scheduler() {
     max_views = std::max<uint64_t>(max_views, k);
     const bool packed = cfg.precision != 0;
     lk.unlock();
-    cudaError_t e = cudaMemcpyAsync(L.d_views, L.h_views, k * sizeof(ViewDesc), cudaMemcpyHostToDevice, L.st);
+    cudaError_t e = cudaMemcpyAsync(L.d_views, L.h_views, k * kTableEntry, cudaMemcpyHostToDevice, L.st);
     if (e == cudaSuccess) e = cudaMemsetAsync(L.d_queue, 0, kQueueBytes, L.st);
     if (e == cudaSuccess)
-      e = launch_multi(d_scenes, packed, L.d_views, (int)k, (uint32_t)cbase, d_arena, L.d_queue, d_status, L.st);
+      e = launch_multi(d_scenes, packed, L.d_views, (int)k, (uint32_t)cbase,
+                       reinterpret_cast<float* const*>(L.d_views + k), L.d_queue, d_status, L.st);
     if (e == cudaSuccess) e = cudaEventRecord(L.ev, L.st);
     lk.lock();
     if (e != cudaSuccess) {
@@ -253,12 +268,12 @@ void kdgr_server_s::completer() {
     lk.unlock();
     cudaError_t e = cudaEventSynchronize(L.ev);
     for (Request* r : L.reqs)
-      if (e == cudaSuccess)
+      if (e == cudaSuccess && !r->direct)
         e = cudaMemcpy(r->host_rgb, d_arena + 3 * r->dev_off, 12ull * r->pixels, cudaMemcpyDeviceToHost);
     lk.lock();
     const Clock::time_point now = Clock::now();
     for (Request* r : L.reqs) {
-      arena.release(r->dev_off, r->pixels);
+      if (!r->direct) arena.release(r->dev_off, r->pixels);
       --slots[r->slot].inflight;
       r->state = kDone;
       r->t_done = now;
@@ -330,8 +345,8 @@ int kdgr_server_create(const kdgr_server_config* cfg, kdgr_server_t* out) {
   for (Lane& L : s->lanes) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaMalloc(&L.d_views, sizeof(ViewDesc) * c.max_views_per_launch);
-    if (e == cudaSuccess) e = cudaMallocHost(&L.h_views, sizeof(ViewDesc) * c.max_views_per_launch);
+    if (e == cudaSuccess) e = cudaMalloc(&L.d_views, kTableEntry * c.max_views_per_launch);
+    if (e == cudaSuccess) e = cudaMallocHost(&L.h_views, kTableEntry * c.max_views_per_launch);
     if (e == cudaSuccess) e = cudaMalloc(&L.d_queue, kQueueBytes);
   }
   if (e != cudaSuccess) {
@@ -354,6 +369,7 @@ int kdgr_server_add_scene(kdgr_server_t s, const uint32_t* nodes, uint32_t n_nod
     set_error("kdgr_server_add_scene: null argument");
     return KDGR_ERR_INVALID_ARG;
   }
+  DeviceScope ds(s->device);  // the scene lives on the server's device
   const bool packed = s->cfg.precision != 0;
   int slot = -1;
   {
@@ -449,6 +465,20 @@ int kdgr_server_submit(kdgr_server_t s, int slot, const kdgr_view* views, int n_
     r->pixels = std::max<uint64_t>(r->pixels, v.out_offset + (uint64_t)v.width * v.height);
     r->rays += (uint64_t)v.width * v.height;
   }
+  {
+    // page-locked from the first float to the last: written by the kernel
+    DeviceScope ds(s->device);
+    const float* last = host_rgb + 3 * r->pixels - 1;
+    cudaPointerAttributes a{}, b{};
+    if (ds.err == cudaSuccess && cudaPointerGetAttributes(&a, host_rgb) == cudaSuccess &&
+        cudaPointerGetAttributes(&b, last) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+        b.type == cudaMemoryTypeHost && a.devicePointer &&
+        (const char*)b.devicePointer - (const char*)a.devicePointer == (const char*)last - (const char*)host_rgb) {
+      r->direct = true;
+      r->out_dev = static_cast<float*>(a.devicePointer);
+    }
+    cudaGetLastError();  // a pageable pointer is not an error of this call
+  }
   std::lock_guard<std::mutex> lk(s->mu);
   if (s->fatal != KDGR_OK) {
     set_error(s->fatal_msg);
@@ -458,7 +488,7 @@ int kdgr_server_submit(kdgr_server_t s, int slot, const kdgr_view* views, int n_
     set_error("kdgr_server_submit: no scene in slot " + std::to_string(slot));
     return KDGR_ERR_INVALID_ARG;
   }
-  if (((r->pixels + 63) & ~uint64_t(63)) > s->arena.total) {
+  if (!r->direct && ((r->pixels + 63) & ~uint64_t(63)) > s->arena.total) {
     set_error("kdgr_server_submit: request output exceeds the arena (HBM budget)");
     return KDGR_ERR_BUDGET;
   }
@@ -579,6 +609,7 @@ int kdgr_server_destroy(kdgr_server_t s) {
   }
   if (s->sched.joinable()) s->sched.join();
   if (s->compl_.joinable()) s->compl_.join();
+  DeviceScope ds(s->device);
   for (Lane& L : s->lanes) {
     if (L.st) cudaStreamSynchronize(L.st);
     if (L.st) cudaStreamDestroy(L.st);

@@ -131,9 +131,10 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
                          cudaStream_t st);
 int batch_sms();
 // Multi-scene persistent launch (warp-strip schedule) for the serving loop;
-// views[].scene indexes d_scenes.
+// views[v].scene indexes d_scenes and d_outs[v] is view v's output base.
 cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* d_views, int n_views,
-                         uint32_t total_blocks, float* rgb, uint32_t* queue, uint32_t* status, cudaStream_t st);
+                         uint32_t total_blocks, float* const* d_outs, uint32_t* queue, uint32_t* status,
+                         cudaStream_t st);
 // Scale ratio above which a Gaussian's factors come from the FP64 precompute.
 constexpr double kAnisoRatio = 1e3;
 

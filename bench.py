@@ -49,6 +49,7 @@ path (views are independent), weak scaling.
 from __future__ import annotations
 
 import argparse
+import collections
 import importlib
 import json
 import os
@@ -474,11 +475,64 @@ def poisson_requests(rate: float, seconds: float, n_scenes: int, seed: int):
         out.append((t, int(rng.integers(0, n_scenes)), cams))
 
 
+class PinnedRing:
+    """Output buffers of the served client: ranges of one page-locked slab,
+    handed out in submission order and given back when their request has
+    been waited for.  The server's kernel writes page-locked buffers
+    directly.  When the slab is full the client waits for its oldest
+    request first (time reported as client_wait_s: non-zero only when the
+    offered load exceeds what the GPU serves)."""
+
+    def __init__(self, torch, n_floats: int):
+        self.slab = torch.empty(n_floats, dtype=torch.float32, pin_memory=True)
+        self.n = n_floats
+        self.live = collections.deque()  # (start, end, ticket)
+        self.head = 0
+        self.waited = 0.0
+
+    def _retire_oldest(self, srv):
+        _, _, t = self.live.popleft()
+        t0 = time.perf_counter()
+        rc, _ = srv.wait(t, timeout_ms=600_000)
+        self.waited += time.perf_counter() - t0
+        assert rc == 0, rc
+        if not self.live:
+            self.head = 0
+
+    def take(self, srv, n: int):
+        """A slab range of n floats; returns (start, view)."""
+        assert n <= self.n
+        while True:
+            tail = self.live[0][0] if self.live else 0
+            if not self.live or self.head > tail:
+                if self.head + n <= self.n:
+                    start = self.head
+                    break
+                if self.live and n < tail:
+                    start = 0
+                    break
+            elif self.head + n < tail:
+                start = self.head
+                break
+            self._retire_oldest(srv)
+        self.head = start + n
+        return start, self.slab[start:start + n]
+
+    def add(self, start: int, n: int, ticket: int):
+        self.live.append((start, start + n, ticket))
+
+    def drain(self, srv):
+        while self.live:
+            self._retire_oldest(srv)
+
+
 def run_serving_rates(pkg, rates, seconds):
     """Four resident scenes (0.5M/1M/2M/3M cluster+shell, seeds 1-4) under a
     60 GB budget; Poisson request streams at each rate, served by the
     continuous-batching server, and by the plain per-request path (one
-    request at a time, one plain-kernel launch per view) for comparison."""
+    request at a time, one plain-kernel launch per view) for comparison.
+    Both clients receive frames in page-locked host memory written by the
+    kernels themselves."""
     import threading
     import torch
     F = pkg.renderer
@@ -495,25 +549,25 @@ def run_serving_rates(pkg, rates, seconds):
     setup = {"seconds": round(time.time() - t0, 1), "resident_gb": round(srv.stats()["resident_bytes"] / 1e9, 2),
              "budget_gb": 60.0 * (1 << 30) / 1e9}
     log(f"[bench] serving: 4 scenes built and resident in {setup['seconds']}s, {setup['resident_gb']} GB")
+    max_req = 16 * 1920 * 1080 * 3  # floats of the largest request
+    ring = PinnedRing(torch, 1 << 30)  # 4 GiB of served output in flight
+    plain_out = torch.empty(max_req, dtype=torch.float32, pin_memory=True)
     results = {}
     for rate in rates:
         reqs = poisson_requests(rate, seconds, len(sizes), seed=int(rate))
         rays = sum(w * h for _, _, cams in reqs for _, w, h in cams)
         # served
         srv.reset_stats()
-        bufs, tickets = [], []
+        ring.waited = 0.0
         start = time.time()
         for arr, scene, cams in reqs:
             now = time.time() - start
             if arr > now:
                 time.sleep(arr - now)
             views, total, _ = F.make_views(cams)
-            buf = np.empty(total * 3, np.float32)
-            bufs.append(buf)
-            tickets.append(srv.submit(slots[scene], views, len(cams), buf))
-        for t in tickets:
-            rc, _ = srv.wait(t, timeout_ms=600_000)
-            assert rc == 0
+            off, buf = ring.take(srv, total * 3)
+            ring.add(off, total * 3, srv.submit(slots[scene], views, len(cams), buf))
+        ring.drain(srv)
         st = srv.stats()
         # plain path: FIFO, one request at a time, plain kernel per view
         dev = torch.device("cuda:0")
@@ -531,10 +585,10 @@ def run_serving_rates(pkg, rates, seconds):
                     time.sleep(0.0005)
                     continue
                 arr_abs, scene, cams = item
+                off = 0
                 for cam, w, h in cams:
-                    out = torch.empty(w * h * 3, device=dev)
-                    plain_scenes[scene].render(cam, w, h, out)
-                    out.cpu()
+                    plain_scenes[scene].render(cam, w, h, plain_out[off:off + w * h * 3])
+                    off += w * h * 3
                 stream.synchronize()
                 lat.append(1e3 * (time.time() - arr_abs))
 
@@ -556,7 +610,8 @@ def run_serving_rates(pkg, rates, seconds):
             "requests": len(reqs), "rays": int(rays),
             "served": {"p50_ms": round(st["p50_ms"], 2), "p99_ms": round(st["p99_ms"], 2),
                        "mean_ms": round(st["mean_ms"], 2), "mrays_per_s": round(st["mrays_per_s"], 1),
-                       "launches": st["launches"], "max_views_per_launch": st["max_views_per_launch"]},
+                       "launches": st["launches"], "max_views_per_launch": st["max_views_per_launch"],
+                       "client_wait_s": round(ring.waited, 3)},
             "plain": {"p50_ms": round(pct(lat, 0.5), 2), "p99_ms": round(pct(lat, 0.99), 2),
                       "mrays_per_s": round(rays / plain_wall / 1e6, 1)},
         }

@@ -363,8 +363,11 @@ int kdgr_server_add_scene(kdgr_server_t server, const uint32_t* nodes, uint32_t 
  * (at most 60 s) for launches that use it. */
 int kdgr_server_remove_scene(kdgr_server_t server, int slot);
 /* Queue a request.  host_rgb receives 3 floats per pixel at each view's
- * out_offset (rows flipped per view); pinned memory copies fastest.  Returns
- * KDGR_ERR_BUDGET when the request's output can never fit the arena. */
+ * out_offset (rows flipped per view).  Page-locked host_rgb (cudaMallocHost,
+ * cudaHostRegister) is written by the render kernel itself and takes no
+ * arena space; pageable host_rgb is rendered into the arena and copied out
+ * when the launch completes.  Returns KDGR_ERR_BUDGET when a pageable
+ * request's output can never fit the arena. */
 int kdgr_server_submit(kdgr_server_t server, int slot, const kdgr_view* views, int n_views, float* host_rgb,
                        uint64_t* ticket);
 /* Wait (at most timeout_ms) for a request; returns its status (KDGR_OK,
