@@ -47,7 +47,7 @@ using Clock = std::chrono::steady_clock;
 
 namespace {
 
-constexpr int kMaxSlots = 64;
+constexpr int kMaxSlots = kSceneSlots;
 // launch-table bytes per view: its ViewDesc and its output base
 constexpr size_t kTableEntry = sizeof(ViewDesc) + sizeof(float*);
 static_assert(sizeof(ViewDesc) % alignof(float*) == 0, "output bases follow the views");
@@ -135,7 +135,7 @@ struct kdgr_server_s {
   std::condition_variable cv_sched, cv_compl, cv_done;
   bool stop = false;
   Slot slots[kMaxSlots];
-  FastView* d_scenes = nullptr;
+  SceneTable table{};  // device views of the slots' scenes (launch parameters)
   uint64_t resident = 0;
   float* d_arena = nullptr;
   Arena arena;
@@ -237,11 +237,12 @@ void kdgr_server_s::scheduler() {
     views_launched += k;
     max_views = std::max<uint64_t>(max_views, k);
     const bool packed = cfg.precision != 0;
+    const SceneTable tbl = table;  // add_scene may fill another slot meanwhile
     lk.unlock();
     cudaError_t e = cudaMemcpyAsync(L.d_views, L.h_views, k * kTableEntry, cudaMemcpyHostToDevice, L.st);
     if (e == cudaSuccess) e = cudaMemsetAsync(L.d_queue, 0, kQueueBytes, L.st);
     if (e == cudaSuccess)
-      e = launch_multi(d_scenes, packed, L.d_views, (int)k, (uint32_t)cbase,
+      e = launch_multi(tbl, packed, L.d_views, (int)k, (uint32_t)cbase,
                        reinterpret_cast<float* const*>(L.d_views + k), L.d_queue, d_status, L.st);
     if (e == cudaSuccess) e = cudaEventRecord(L.ev, L.st);
     lk.lock();
@@ -337,10 +338,8 @@ int kdgr_server_create(const kdgr_server_config* cfg, kdgr_server_t* out) {
   }
   cudaGetDevice(&s->device);
   cudaError_t e = cudaMalloc(&s->d_arena, c.arena_bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&s->d_scenes, sizeof(FastView) * kMaxSlots);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_status, 4);
   if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, 4);
-  if (e == cudaSuccess) e = cudaMemset(s->d_scenes, 0, sizeof(FastView) * kMaxSlots);
   s->lanes.resize(c.lanes);
   for (Lane& L : s->lanes) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking);
@@ -405,12 +404,7 @@ int kdgr_server_add_scene(kdgr_server_t s, const uint32_t* nodes, uint32_t n_nod
     set_error("kdgr_server_add_scene: scene exceeds the HBM budget");
     return KDGR_ERR_BUDGET;
   }
-  const FastView fv = sc->fast_view(s->cfg.precision != 0);
-  cudaError_t e = cudaMemcpy(s->d_scenes + slot, &fv, sizeof(FastView), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
-    kdgr_scene_destroy(sc);
-    return cuda_fail(e, "kdgr_server_add_scene");
-  }
+  s->table.s[slot] = sc->fast_view(s->cfg.precision != 0);
   s->slots[slot].scene = sc;
   s->slots[slot].bytes = info.device_bytes;
   s->resident += info.device_bytes;
@@ -438,6 +432,7 @@ int kdgr_server_remove_scene(kdgr_server_t s, int slot) {
   for (Request* r : std::vector<Request*>(s->queue.begin(), s->queue.end()))
     if (r->slot == slot) r->cancel = true;
   kdgr_scene_destroy(s->slots[slot].scene);
+  s->table.s[slot] = FastView{};
   s->resident -= s->slots[slot].bytes;
   s->slots[slot] = Slot();
   s->slots[slot].removing = false;
@@ -621,7 +616,6 @@ int kdgr_server_destroy(kdgr_server_t s) {
   for (Slot& sl : s->slots)
     if (sl.scene) kdgr_scene_destroy(sl.scene);
   if (s->d_arena) cudaFree(s->d_arena);
-  if (s->d_scenes) cudaFree(s->d_scenes);
   if (s->d_status) cudaFree(s->d_status);
   delete s;
   return KDGR_OK;

@@ -1027,13 +1027,14 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
 
 // Multi-scene form of the warp-strip schedule for the serving loop: every
 // view names a scene slot and each warp renders its quarter-block against
-// that slot's arrays (scenes[] in device memory).  One persistent launch
+// that slot's arrays (the slot table travels in the launch parameters, so
+// the warp-uniform field reads hit the constant cache).  One persistent launch
 // serves the requests of all resident scenes queued in a tick.  Items are
 // quarters of 16x8 blocks; queue word 1 + k counts the claims of strip k.
 // outs[v] is view v's output base (the device arena, or a request's
 // page-locked host buffer); the view's out_off counts pixels from it.
 template <bool PACKED>
-__global__ void __launch_bounds__(kThreads, 8) k_render_multi(const FastView* __restrict__ scenes,
+__global__ void __launch_bounds__(kThreads, 8) k_render_multi(const __grid_constant__ SceneTable scenes,
                                                               const ViewDesc* __restrict__ views, int n_views,
                                                               uint32_t total_items, float* const* __restrict__ outs,
                                                               uint32_t* queue, uint32_t* status, int n_strips) {
@@ -1058,7 +1059,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_render_multi(const FastView* __
     const uint32_t blk = it >> 2;
     const int vi = find_view(views, n_views, blk, KDGR_SCHED_CTA_BLOCKS);
     const ViewDesc& V = views[vi];
-    const FastView& S = scenes[__ldg(&V.scene)];
+    const FastView& S = scenes.s[__ldg(&V.scene) & (kSceneSlots - 1)];
     float* const rgb = outs[vi];
     const uint32_t lb = blk - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
     int x, y;
@@ -1472,7 +1473,7 @@ cudaError_t build_flag_pairs(const uint32_t* d_gid, uint32_t n_entries, const ui
 
 int batch_sms() { return num_sms(); }
 
-cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* d_views, int n_views,
+cudaError_t launch_multi(const SceneTable& scenes, bool packed, const ViewDesc* d_views, int n_views,
                          uint32_t total_blocks, float* const* d_outs, uint32_t* queue, uint32_t* status,
                          cudaStream_t st) {
   auto fn = packed ? k_render_multi<true> : k_render_multi<false>;
@@ -1484,7 +1485,7 @@ cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* 
   uint64_t blocks = (uint64_t)num_sms() * (occ > 0 ? occ : 1);
   const uint64_t cap = ((uint64_t)quarters + kWarps - 1) / kWarps;
   if (blocks > cap) blocks = cap > 0 ? cap : 1;
-  fn<<<(unsigned)blocks, kThreads, 0, st>>>(d_scenes, d_views, n_views, quarters, d_outs, queue, status,
+  fn<<<(unsigned)blocks, kThreads, 0, st>>>(scenes, d_views, n_views, quarters, d_outs, queue, status,
                                             std::min(num_sms(), kMaxStrips));
   return cudaGetLastError();
 }

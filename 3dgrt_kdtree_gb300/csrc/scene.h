@@ -130,9 +130,16 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
                          const uint32_t totals[3], float* rgb, float* alpha, float* depth, uint32_t* queue,
                          cudaStream_t st);
 int batch_sms();
+// The serving loop's scene slots, passed whole in the parameters of each
+// multi-scene launch (7.7 KB): a warp reads its scene's fields from the
+// constant bank rather than from a table in global memory.
+constexpr int kSceneSlots = 64;
+struct SceneTable {
+  FastView s[kSceneSlots];
+};
 // Multi-scene persistent launch (warp-strip schedule) for the serving loop;
-// views[v].scene indexes d_scenes and d_outs[v] is view v's output base.
-cudaError_t launch_multi(const FastView* d_scenes, bool packed, const ViewDesc* d_views, int n_views,
+// views[v].scene indexes the table and d_outs[v] is view v's output base.
+cudaError_t launch_multi(const SceneTable& scenes, bool packed, const ViewDesc* d_views, int n_views,
                          uint32_t total_blocks, float* const* d_outs, uint32_t* queue, uint32_t* status,
                          cudaStream_t st);
 // Scale ratio above which a Gaussian's factors come from the FP64 precompute.
