@@ -925,6 +925,42 @@ __device__ __forceinline__ void group_pixel(int bx, int by, int q, int lane, int
 //               its four warps render the four quarters, so the rays sharing
 //               the SM's L1 are neighbours.
 // MINB caps registers so that MINB CTAs fit per SM (0: compiler's choice).
+// Strip k of n over total items: [total * k / n, total * (k + 1) / n).
+__device__ __forceinline__ uint32_t strip_lo(uint32_t total, uint32_t n, uint32_t k) {
+  return (uint32_t)((uint64_t)total * k / n);
+}
+
+// The first strip after k in visiting order (k + 1, k + 2, ... mod n) whose
+// claim counter (queue word 1 + j) is still below its size, or n when every
+// strip is exhausted; called by a whole warp.  The lanes read the counters
+// together, from L2 (they move by atomics, so not through L1), one load
+// each per 32 strips, all issued before the first vote.  Trying the strips
+// one claim at a time instead cost a warp up to n sequential atomic round
+// trips at the end of a launch, after its last item.  A strip read as open
+// may be exhausted by the time the caller claims from it; the caller then
+// asks again, and since a counter only grows, every failed claim closes a
+// strip for good.
+__device__ __forceinline__ uint32_t next_open_strip(const uint32_t* queue, uint32_t total, uint32_t n, uint32_t k,
+                                                    unsigned lane) {
+  constexpr int kRounds = (kMaxStrips + 31) / 32;
+  bool open[kRounds];
+#pragma unroll
+  for (int r = 0; r < kRounds; ++r) {
+    const uint32_t off = 1u + 32u * r + lane;  // off == n is k itself
+    open[r] = false;
+    if (off <= n) {
+      const uint32_t j = (k + off) % n;
+      open[r] = __ldcg(queue + 1 + j) < strip_lo(total, n, j + 1) - strip_lo(total, n, j);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kRounds; ++r) {
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, open[r]);
+    if (m) return (k + 1u + 32u * r + (uint32_t)(__ffs(m) - 1)) % n;
+  }
+  return n;
+}
+
 template <bool PACKED, int SCHED, int MINB, int KB, bool PKT, int LPR>
 __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, const ViewDesc* __restrict__ views,
                                                                  int n_views, uint32_t total_items,
@@ -944,15 +980,16 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
     uint32_t smid;
     asm("mov.u32 %0, %%smid;" : "=r"(smid));
     const uint32_t n = (uint32_t)chunk;  // number of strips
-    uint32_t k = smid % n, visited = 0;
-    while (visited < n) {
-      const uint32_t b0 = (uint32_t)((uint64_t)total_items * k / n), b1 = (uint32_t)((uint64_t)total_items * (k + 1) / n);
+    uint32_t k = smid % n, fails = 0;
+    while (fails <= n) {  // a warp's claims fail at most once per strip
+      const uint32_t b0 = strip_lo(total_items, n, k), b1 = strip_lo(total_items, n, k + 1);
       uint32_t it = 0;
       if (lane == 0) it = b0 + atomicAdd(queue + 1 + k, 1u);
       it = __shfl_sync(0xFFFFFFFFu, it, 0);
       if (it >= b1) {
-        k = (k + 1) % n;
-        ++visited;
+        ++fails;
+        k = next_open_strip(queue, total_items, n, k, (unsigned)lane);
+        if (k >= n) break;
         continue;
       }
       const uint32_t blk = it / (4u * LPR), q = it % (4u * LPR);
@@ -971,22 +1008,32 @@ __global__ void __launch_bounds__(kThreads, MINB) k_render_batch(FastView S, con
     asm("mov.u32 %0, %%smid;" : "=r"(smid));
     const uint32_t n = (uint32_t)chunk;  // number of strips (the SM count; chunk is reused for it)
     if (tid == 0) s_strip = smid % n;
-    uint32_t visited = 0;  // strips tried so far by this CTA (uniform)
-    while (visited < n) {
+    while (true) {
       __syncthreads();
-      if (tid == 0) {
-        const uint32_t k = s_strip;
-        const uint32_t b0 = (uint32_t)((uint64_t)total_items * k / n), b1 = (uint32_t)((uint64_t)total_items * (k + 1) / n);
-        const uint32_t it = b0 + atomicAdd(queue + 1 + k, 1u);
-        s_work = it < b1 ? it : 0xFFFFFFFFu;
-        if (it >= b1) s_strip = (k + 1) % n;  // this strip is done: move on to the next one
+      if (warp == 0) {
+        // claim the next item of this CTA's strip, or move on to the next
+        // strip with items left (a failed claim closes its strip for good)
+        uint32_t k = s_strip, item = 0xFFFFFFFFu;
+        for (uint32_t fails = 0; fails <= n; ++fails) {
+          const uint32_t b0 = strip_lo(total_items, n, k), b1 = strip_lo(total_items, n, k + 1);
+          uint32_t it = 0;
+          if (lane == 0) it = b0 + atomicAdd(queue + 1 + k, 1u);
+          it = __shfl_sync(0xFFFFFFFFu, it, 0);
+          if (it < b1) {
+            item = it;
+            break;
+          }
+          k = next_open_strip(queue, total_items, n, k, (unsigned)lane);
+          if (k >= n) break;
+        }
+        if (lane == 0) {
+          s_work = item;
+          if (k < n) s_strip = k;
+        }
       }
       __syncthreads();
       const uint32_t item = s_work;
-      if (item == 0xFFFFFFFFu) {
-        ++visited;
-        continue;
-      }
+      if (item == 0xFFFFFFFFu) break;
       const ViewDesc& V = views[find_view(views, n_views, item, KDGR_SCHED_CTA_BLOCKS)];
       const uint32_t lb = item - __ldg(&V.cb_base), nx = __ldg(&V.cb_x);
       int x, y;
@@ -1045,15 +1092,16 @@ __global__ void __launch_bounds__(kThreads, 8) k_render_multi(const __grid_const
   uint32_t smid;
   asm("mov.u32 %0, %%smid;" : "=r"(smid));
   const uint32_t n = (uint32_t)n_strips;
-  uint32_t k = smid % n, visited = 0;
-  while (visited < n) {
-    const uint32_t b0 = (uint32_t)((uint64_t)total_items * k / n), b1 = (uint32_t)((uint64_t)total_items * (k + 1) / n);
+  uint32_t k = smid % n, fails = 0;
+  while (fails <= n) {  // a warp's claims fail at most once per strip
+    const uint32_t b0 = strip_lo(total_items, n, k), b1 = strip_lo(total_items, n, k + 1);
     uint32_t it = 0;
     if (lane == 0) it = b0 + atomicAdd(queue + 1 + k, 1u);
     it = __shfl_sync(0xFFFFFFFFu, it, 0);
     if (it >= b1) {
-      k = (k + 1) % n;
-      ++visited;
+      ++fails;
+      k = next_open_strip(queue, total_items, n, k, (unsigned)lane);
+      if (k >= n) break;
       continue;
     }
     const uint32_t blk = it >> 2;

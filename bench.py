@@ -486,16 +486,18 @@ class PinnedRing:
     def __init__(self, torch, n_floats: int):
         self.slab = torch.empty(n_floats, dtype=torch.float32, pin_memory=True)
         self.n = n_floats
-        self.live = collections.deque()  # (start, end, ticket)
+        self.live = collections.deque()  # (start, end, ticket, submit delay s)
         self.head = 0
         self.waited = 0.0
+        self.lat_ms = []  # per request: scheduled arrival -> done
 
     def _retire_oldest(self, srv):
-        _, _, t = self.live.popleft()
+        _, _, t, delay = self.live.popleft()
         t0 = time.perf_counter()
-        rc, _ = srv.wait(t, timeout_ms=600_000)
+        rc, st = srv.wait(t, timeout_ms=600_000)
         self.waited += time.perf_counter() - t0
         assert rc == 0, rc
+        self.lat_ms.append(1e3 * delay + st["latency_ms"])
         if not self.live:
             self.head = 0
 
@@ -518,8 +520,9 @@ class PinnedRing:
         self.head = start + n
         return start, self.slab[start:start + n]
 
-    def add(self, start: int, n: int, ticket: int):
-        self.live.append((start, start + n, ticket))
+    def add(self, start: int, n: int, ticket: int, delay: float):
+        """delay: seconds from the request's scheduled arrival to its submit."""
+        self.live.append((start, start + n, ticket, delay))
 
     def drain(self, srv):
         while self.live:
@@ -549,9 +552,20 @@ def run_serving_rates(pkg, rates, seconds):
     setup = {"seconds": round(time.time() - t0, 1), "resident_gb": round(srv.stats()["resident_bytes"] / 1e9, 2),
              "budget_gb": 60.0 * (1 << 30) / 1e9}
     log(f"[bench] serving: 4 scenes built and resident in {setup['seconds']}s, {setup['resident_gb']} GB")
+    pct = lambda v, p: v[min(len(v) - 1, int(p * (len(v) - 1) + 0.5))]
     max_req = 16 * 1920 * 1080 * 3  # floats of the largest request
     ring = PinnedRing(torch, 1 << 30)  # 4 GiB of served output in flight
     plain_out = torch.empty(max_req, dtype=torch.float32, pin_memory=True)
+    # untimed warm-up, one small request per scene through both paths
+    # (first launches load their kernels and run one-time queries)
+    for i, slot in enumerate(slots):
+        cams = [(pkg.scenes.front_camera(256, 256), 256, 256)]
+        views, total, _ = F.make_views(cams)
+        off, buf = ring.take(srv, total * 3)
+        ring.add(off, total * 3, srv.submit(slot, views, 1, buf), 0.0)
+        plain_scenes[i].render(cams[0][0], 256, 256, plain_out[:total * 3])
+    ring.drain(srv)
+    torch.cuda.synchronize()
     results = {}
     for rate in rates:
         reqs = poisson_requests(rate, seconds, len(sizes), seed=int(rate))
@@ -559,6 +573,7 @@ def run_serving_rates(pkg, rates, seconds):
         # served
         srv.reset_stats()
         ring.waited = 0.0
+        ring.lat_ms = []
         start = time.time()
         for arr, scene, cams in reqs:
             now = time.time() - start
@@ -566,9 +581,11 @@ def run_serving_rates(pkg, rates, seconds):
                 time.sleep(arr - now)
             views, total, _ = F.make_views(cams)
             off, buf = ring.take(srv, total * 3)
-            ring.add(off, total * 3, srv.submit(slots[scene], views, len(cams), buf))
+            ticket = srv.submit(slots[scene], views, len(cams), buf)
+            ring.add(off, total * 3, ticket, max(0.0, time.time() - start - arr))
         ring.drain(srv)
         st = srv.stats()
+        served_lat = sorted(ring.lat_ms)
         # plain path: FIFO, one request at a time, plain kernel per view
         dev = torch.device("cuda:0")
         q, lat, lock = [], [], threading.Lock()
@@ -605,10 +622,13 @@ def run_serving_rates(pkg, rates, seconds):
         th.join()
         plain_wall = time.time() - start
         lat.sort()
-        pct = lambda v, p: v[min(len(v) - 1, int(p * (len(v) - 1) + 0.5))]
         results[str(int(rate))] = {
             "requests": len(reqs), "rays": int(rays),
-            "served": {"p50_ms": round(st["p50_ms"], 2), "p99_ms": round(st["p99_ms"], 2),
+            # latency from the request's scheduled arrival, as for plain;
+            # server_* from its submit (later than arrival only while the
+            # client waits for output space: client_wait_s)
+            "served": {"p50_ms": round(pct(served_lat, 0.5), 2), "p99_ms": round(pct(served_lat, 0.99), 2),
+                       "server_p50_ms": round(st["p50_ms"], 2), "server_p99_ms": round(st["p99_ms"], 2),
                        "mean_ms": round(st["mean_ms"], 2), "mrays_per_s": round(st["mrays_per_s"], 1),
                        "launches": st["launches"], "max_views_per_launch": st["max_views_per_launch"],
                        "client_wait_s": round(ring.waited, 3)},
