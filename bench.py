@@ -124,35 +124,56 @@ def common_config(desc: dict, world: int) -> dict:
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
-    """nvidia-smi samples during the timed region."""
+    """nvidia-smi samples (every 20 ms), each stamped with the host clock as
+    it arrives; `stop(t0, t1)` keeps the samples taken inside the timed
+    window [t0, t1] (host time.time()).  Started before the warm-up, so the
+    sampler is running when the timed region begins."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
-        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        import threading
+        self.rows = []
+        self.first = threading.Event()
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
-                                      stderr=subprocess.DEVNULL)
+                                       "--format=csv,noheader,nounits", "-lms", "20"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
+            return
 
-    def stop(self) -> dict:
+        def reader():
+            for line in self.p.stdout:
+                if line.strip():
+                    self.rows.append((time.time(), line.split(",")))
+                    self.first.set()
+
+        self.th = threading.Thread(target=reader, daemon=True)
+        self.th.start()
+        self.first.wait(10.0)
+
+    def stop(self, t0: float = None, t1: float = None) -> dict:
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.05)  # the sample after the window's end
         self.p.terminate()
         self.p.wait()
-        self.f.flush()
-        rows = [l.split(",") for l in open(self.f.name).read().strip().splitlines() if l.strip()]
-        os.unlink(self.f.name)
-        sm = [float(r[0]) for r in rows if len(r) >= 8 and r[0].strip().replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in rows if len(r) >= 8 and r[1].strip().replace(".", "").isdigit()]
+        self.th.join(2.0)
+        ok = [(ts, r) for ts, r in self.rows if len(r) >= 8 and r[0].strip().replace(".", "").isdigit()]
+        window = "timed region"
+        rows = [r for ts, r in ok if t0 is None or t0 <= ts <= t1]
+        if not rows and ok and t0 is not None:  # a region shorter than the interval: the nearest samples
+            ok.sort(key=lambda x: min(abs(x[0] - t0), abs(x[0] - t1)))
+            rows, window = [r for _, r in ok[:2]], "nearest samples to a timed region shorter than the interval"
+        sm = [float(r[0]) for r in rows]
+        mx = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows if len(r) >= 8 for i in range(4) if "Active" in r[4 + i]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[4 + i]
                           and "Not" not in r[4 + i]})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(sm)}
+                "reasons": reasons, "samples": len(sm), "interval_ms": 20, "window": window}
 
 
 # ------------------------------------------------------------------ roofline
@@ -292,17 +313,17 @@ def run_ours(args, rank: int, world: int):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
+    clocks = ClockSampler(dev.index)
     for _ in range(args.warmup):
         batch.run()
     torch.cuda.synchronize(dev)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
-    clocks = ClockSampler(dev.index)
     wall0 = time.time()
     ms = timed_loop(batch.run, args.steps, flush, stream, dev)
     wall = time.time() - wall0
-    clk = clocks.stop()
+    clk = clocks.stop(wall0, wall0 + wall)
     if world > 1:
         torch.distributed.barrier()
     assert scene.status() == 0, "kernel raised an error status"
@@ -878,11 +899,12 @@ def run_hybrid(args):
             out.append(a.elapsed_time(b))
         return sum(out) / len(out)
 
+    clocks = ClockSampler(0)
     for _ in range(args.warmup):
         scene.render_hybrid(cam, w, h, sec, rgb)
-    clocks = ClockSampler(0)
+    t0 = time.time()
     ms = timed(lambda: scene.render_hybrid(cam, w, h, sec, rgb), args.steps)
-    clk = clocks.stop()
+    clk = clocks.stop(t0, time.time())
     torch.cuda.synchronize(dev)
     hyb = rgb.cpu().numpy().copy()
     for _ in range(args.warmup):
@@ -916,7 +938,7 @@ def run_hybrid(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="scale",
                     choices=["scale", "small", "mid", "batching", "precision", "serving", "build", "hybrid"])
