@@ -1521,6 +1521,37 @@ cudaError_t build_flag_pairs(const uint32_t* d_gid, uint32_t n_entries, const ui
 
 int batch_sms() { return num_sms(); }
 
+namespace {
+constexpr int kStageViews = 256;
+struct ViewStage {
+  ViewDesc views[kStageViews];
+  int32_t n_views;
+};
+static_assert(sizeof(ViewStage) <= 32764, "kernel parameters are limited to 32,764 bytes");
+static_assert(kQueueBytes / sizeof(uint32_t) <= 256, "queue words are zeroed by one 256-thread block");
+
+__global__ void __launch_bounds__(256) k_stage_views(const __grid_constant__ ViewStage p, ViewDesc* table,
+                                                     uint32_t* queue) {
+  const int i = threadIdx.x;
+  if (i < p.n_views) table[i] = p.views[i];
+  if (i < (int)(kQueueBytes / sizeof(uint32_t))) queue[i] = 0u;
+}
+}  // namespace
+
+cudaError_t stage_views(const ViewDesc* views, int n_views, ViewDesc* d_views, uint32_t* d_queue, cudaStream_t st) {
+  if (n_views < 0) return cudaErrorInvalidValue;
+  if (n_views > kStageViews) {
+    cudaError_t e = cudaMemcpyAsync(d_views, views, (size_t)n_views * sizeof(ViewDesc), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_queue, 0, kQueueBytes, st);
+    return e;
+  }
+  ViewStage p;
+  p.n_views = n_views;
+  std::memcpy(p.views, views, (size_t)n_views * sizeof(ViewDesc));
+  k_stage_views<<<1, 256, 0, st>>>(p, d_views, d_queue);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_multi(const SceneTable& scenes, bool packed, const ViewDesc* d_views, int n_views,
                          uint32_t total_blocks, float* const* d_outs, uint32_t* queue, uint32_t* status,
                          cudaStream_t st) {

@@ -130,6 +130,11 @@ cudaError_t launch_batch(kdgr_scene_t s, const kdgr_batch_config& c, const ViewD
                          const uint32_t totals[3], float* rgb, float* alpha, float* depth, uint32_t* queue,
                          cudaStream_t st);
 int batch_sms();
+// Writes a launch's view table to d_views and zeroes its queue words
+// (kQueueBytes at d_queue), stream-ordered: up to 256 views in the
+// parameters of one staging kernel, more by one copy from host memory that
+// must stay valid until the copy has run.
+cudaError_t stage_views(const ViewDesc* views, int n_views, ViewDesc* d_views, uint32_t* d_queue, cudaStream_t st);
 // The serving loop's scene slots, passed whole in the parameters of each
 // multi-scene launch (7.7 KB): a warp reads its scene's fields from the
 // constant bank rather than from a table in global memory.

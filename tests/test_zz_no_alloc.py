@@ -10,9 +10,8 @@ so each call must rewrite the table and zero the counter -- and checked
 against kdgr_render_batch within the parity tolerance of the tests (1e-5
 absolute).  A third test checks the defining property itself: around a
 warmed-up call, the high-water mark of the device's default stream-ordered
-pool (the one kdgr_render_batch draws from) does not rise and the device's
-free memory does not change, while the same probe does see
-kdgr_render_batch's allocation.  The file sorts last so that a run stopping
+pool does not rise and the device's free memory does not change, while the
+same probe does see one stream-ordered allocation from that pool.  The file sorts last so that a run stopping
 at the first failure has already run every other test; it also passes alone
 in a fresh process.
 """
@@ -95,6 +94,12 @@ class _DefaultPool:
     def high(self):
         return self._attr(_USED_MEM_HIGH)
 
+    def alloc_free(self, nbytes, stream):
+        """One stream-ordered allocation and free from this pool."""
+        p = ctypes.c_uint64()
+        assert self.cu.cuMemAllocAsync(ctypes.byref(p), ctypes.c_size_t(nbytes), ctypes.c_void_p(stream)) == 0
+        assert self.cu.cuMemFreeAsync(p, ctypes.c_void_p(stream)) == 0
+
 
 def test_noalloc_takes_no_device_memory(pkg, cuda, fixtures):
     F = pkg.renderer
@@ -111,9 +116,9 @@ def test_noalloc_takes_no_device_memory(pkg, cuda, fixtures):
         assert fn(scene.handle, views, len(cams), rgb.data_ptr(), None, None, None, stream) == 0
         scene.render_batch(views, len(cams), ref)
     torch.cuda.synchronize()
-    # positive control: the allocating entry point raises the pool's high-water mark
+    # positive control: an allocation from the pool raises its high-water mark
     base = pool.reset()
-    scene.render_batch(views, len(cams), ref)
+    pool.alloc_free(1 << 20, stream)
     torch.cuda.synchronize()
     assert pool.high() > base
     free0 = torch.cuda.mem_get_info(cuda)[0]
