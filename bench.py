@@ -16,6 +16,8 @@ A step renders one batch of views of a resident scene.  Configurations:
   serving   4 resident scenes (0.5M/1M/2M/3M), Poisson request streams at
             --rates req/s; p50/p99 latency of the serving loop against the
             plain per-request path
+  serving_1080p  the same for the scale scene alone, requests of 1-16
+            1920x1080 views
   build     kd-tree build time of the scale scene: device builder against
             the host builder, trees compared word for word
   hybrid    secondary-ray renderer on the scale scene (demo spheres and a
@@ -476,10 +478,12 @@ def leg_batching(pkg, scene, tree, rec, dev, flush, stream, args, check: bool):
 
 
 # ------------------------------------------------------------------ serving
-def poisson_requests(rate: float, seconds: float, n_scenes: int, seed: int):
+def poisson_requests(rate: float, seconds: float, n_scenes: int, seed: int, resolutions=None):
     """[(arrival_s, scene, [(Camera, W, H)])]: Poisson arrivals, 1-16 views per
-    request, each view's resolution uniform over the four, scene uniform."""
+    request, each view's resolution uniform over `resolutions` (default: the
+    four of the mixed set), scene uniform."""
     sc = _scenes()
+    res = resolutions or sc.RESOLUTIONS
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
     while True:
@@ -489,7 +493,7 @@ def poisson_requests(rate: float, seconds: float, n_scenes: int, seed: int):
         nv = int(rng.integers(1, 17))
         cams = []
         for _ in range(nv):
-            w, h = sc.RESOLUTIONS[int(rng.integers(0, 4))]
+            w, h = res[int(rng.integers(0, len(res)))]
             d = rng.normal(0.0, 1.0, 3)
             d /= np.linalg.norm(d)
             cams.append((sc.look_at(d * rng.uniform(2.0, 4.0), aspect=w / h), w, h))
@@ -550,9 +554,18 @@ class PinnedRing:
             self._retire_oldest(srv)
 
 
-def run_serving_rates(pkg, rates, seconds):
-    """Four resident scenes (0.5M/1M/2M/3M cluster+shell, seeds 1-4) under a
-    60 GB budget; Poisson request streams at each rate, served by the
+SERVING_SETS = {
+    # the serving config: four scenes, views of the four resolutions
+    "mix": {"sizes": [500_000, 1_000_000, 2_000_000, 3_000_000], "resolutions": None},
+    # the headline config served: the 1M scene, 1920x1080 views
+    "1m_1080p": {"sizes": [1_000_000], "resolutions": [(1920, 1080)]},
+}
+
+
+def run_serving_rates(pkg, rates, seconds, scene_set: str = "mix"):
+    """Resident cluster+shell scenes (the "mix" set: 0.5M/1M/2M/3M, seeds
+    1-4; "1m_1080p": the 1M scene of seed 1 with 1920x1080 views only) under
+    a 60 GB budget; Poisson request streams at each rate, served by the
     continuous-batching server, and by the plain per-request path (one
     request at a time, one plain-kernel launch per view) for comparison.
     Both clients receive frames in page-locked host memory written by the
@@ -561,7 +574,7 @@ def run_serving_rates(pkg, rates, seconds):
     import torch
     F = pkg.renderer
     F.init(0)
-    sizes = [500_000, 1_000_000, 2_000_000, 3_000_000]
+    sizes, resolutions = SERVING_SETS[scene_set]["sizes"], SERVING_SETS[scene_set]["resolutions"]
     srv = F.Server(hbm_budget_bytes=60 << 30, arena_bytes=8 << 30, lanes=3, max_views_per_launch=256)
     plain_scenes, slots = [], []
     t0 = time.time()
@@ -572,7 +585,7 @@ def run_serving_rates(pkg, rates, seconds):
         plain_scenes.append(F.Scene(tree, rec, forms=F.FORM_EXACT))
     setup = {"seconds": round(time.time() - t0, 1), "resident_gb": round(srv.stats()["resident_bytes"] / 1e9, 2),
              "budget_gb": 60.0 * (1 << 30) / 1e9}
-    log(f"[bench] serving: 4 scenes built and resident in {setup['seconds']}s, {setup['resident_gb']} GB")
+    log(f"[bench] serving: {len(sizes)} scenes built and resident in {setup['seconds']}s, {setup['resident_gb']} GB")
     pct = lambda v, p: v[min(len(v) - 1, int(p * (len(v) - 1) + 0.5))]
     max_req = 16 * 1920 * 1080 * 3  # floats of the largest request
     ring = PinnedRing(torch, 1 << 30)  # 4 GiB of served output in flight
@@ -589,7 +602,7 @@ def run_serving_rates(pkg, rates, seconds):
     torch.cuda.synchronize()
     results = {}
     for rate in rates:
-        reqs = poisson_requests(rate, seconds, len(sizes), seed=int(rate))
+        reqs = poisson_requests(rate, seconds, len(sizes), seed=int(rate), resolutions=resolutions)
         rays = sum(w * h for _, _, cams in reqs for _, w, h in cams)
         # served
         srv.reset_stats()
@@ -667,17 +680,20 @@ def run_serving_rates(pkg, rates, seconds):
 
 def run_serving(args):
     pkg = importlib.import_module(PKG)
-    rates = [float(r) for r in args.rates.split(",")]
-    res = run_serving_rates(pkg, rates, args.serve_seconds)
+    hd = args.config == "serving_1080p"
+    rates = [float(r) for r in (args.rates or ("20,40,80,160" if hd else "50,100,200,400")).split(",")]
+    res = run_serving_rates(pkg, rates, args.serve_seconds, "1m_1080p" if hd else "mix")
     results = res["results"]
-    key = "50" if "50" in results else list(results)[0]
+    key = str(int(rates[0]))
+    workload = ("the 1M cluster+shell scene (seed 1) resident, Poisson requests of 1-16 views at 1920x1080"
+                if hd else "4 resident cluster+shell scenes (0.5M/1M/2M/3M), Poisson requests of 1-16 "
+                           "views at 256x256/640x480/1280x720/1920x1080, 60 GB budget")
     return {
         "metric": f"served p99 latency at {key} req/s", "value": results[key]["served"]["p99_ms"], "unit": "ms",
         "n_gpus": 1, "steps": len(rates), "warmup": 0, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "4 resident cluster+shell scenes (0.5M/1M/2M/3M), Poisson requests of 1-16 "
-                               "views at 256x256/640x480/1280x720/1920x1080, 60 GB budget",
-                   "form": "continuous-batching server, 3 lanes", "seconds_per_rate": args.serve_seconds},
+        "config": {"workload": workload, "form": "continuous-batching server, 3 lanes",
+                   "seconds_per_rate": args.serve_seconds},
         "serving": results, "setup": res["setup"],
     }
 
@@ -941,8 +957,11 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="scale",
-                    choices=["scale", "small", "mid", "batching", "precision", "serving", "build", "hybrid"])
-    ap.add_argument("--rates", default="50,100,200,400", help="serving: Poisson request rates (req/s)")
+                    choices=["scale", "small", "mid", "batching", "precision", "serving", "serving_1080p", "build",
+                             "hybrid"])
+    ap.add_argument("--rates", default=None,
+                    help="serving: Poisson request rates (req/s; default 50,100,200,400, or 20,40,80,160 for "
+                         "serving_1080p)")
     ap.add_argument("--serve-seconds", type=float, default=4.0, help="serving: arrivals per rate")
     ap.add_argument("--leg-rate", type=float, default=50.0, help="scale: request rate of the serving leg")
     ap.add_argument("--leg-seconds", type=float, default=3.0, help="scale: arrivals of the serving leg")
@@ -974,7 +993,7 @@ def main():
         out = run_build(args)
     elif args.config == "hybrid":
         out = run_hybrid(args)
-    elif args.config == "serving":
+    elif args.config in ("serving", "serving_1080p"):
         out = run_serving(args)
     else:
         out = run_ours(args, rank, world)
