@@ -103,6 +103,31 @@ def test_batch_output_in_pinned_host_memory(pkg, cuda, fixtures):
     scene.close()
 
 
+@pytest.mark.parametrize("n_views", [1, 256, 257, 300])
+def test_view_table_sizes(pkg, cuda, fixtures, n_views):
+    """kdgr_render_batch stages up to 256 views through a kernel's parameters
+    and copies larger tables; both give the frames of the graph-captured
+    batch, which uploads its table once at creation, and the calls stay
+    repeatable (the scratch comes back from the library's pool)."""
+    fx = fixtures["dense800"]
+    F = pkg.renderer
+    scene = F.Scene(fx.tree, fx.rec)
+    cams = pkg.scenes.sphere_cameras(n_views, seed=31, resolutions=[(16, 16), (24, 8)])
+    views, total, _ = F.make_views(cams)
+    ref = torch.zeros(total * 3, device=cuda)
+    b = F.Batch(scene, views, n_views, ref, None, None, F.BatchConfig.default())
+    b.run()
+    for _ in range(2):
+        rgb = torch.full((total * 3,), -1.0, device=cuda)
+        scene.render_batch(views, n_views, rgb)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(rgb.cpu().numpy(), ref.cpu().numpy())
+    assert float(ref.abs().sum()) > 0
+    assert scene.status() == 0
+    b.close()
+    scene.close()
+
+
 def test_every_schedule_renders_the_same_pixels(pkg, cuda, fixtures):
     """Warp tiles, CTA blocks, SM strips and warp strips (with several chunk sizes and
     register caps) only change which lane renders which pixel; warp packets
