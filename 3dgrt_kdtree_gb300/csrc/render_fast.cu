@@ -373,21 +373,23 @@ struct HitBuf {
   }
   // returns true when an entry fell off the end (the leaf needs another pass)
   __device__ __forceinline__ bool insert(float ct, float cg, uint32_t ci) {
-    bool placed = false;
+    // t is ascending, so c[k] = ct < t[k] is false up to the insertion point
+    // and true after it: every slot takes its old value, the new key or its
+    // left neighbour's old value, decided without a chain between slots
+    bool c[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const bool sw = placed || (ct < t[k]);
-      const float t0 = t[k], g0 = g[k];
-      const uint32_t i0 = i[k];
-      t[k] = sw ? ct : t0;
-      g[k] = sw ? cg : g0;
-      i[k] = sw ? ci : i0;
-      ct = sw ? t0 : ct;
-      cg = sw ? g0 : cg;
-      ci = sw ? i0 : ci;
-      placed = sw;
+    for (int k = 0; k < K; ++k) c[k] = ct < t[k];
+    const float out = c[K - 1] ? t[K - 1] : ct;  // the key that falls off
+#pragma unroll
+    for (int k = K - 1; k > 0; --k) {
+      t[k] = c[k] ? (c[k - 1] ? t[k - 1] : ct) : t[k];
+      g[k] = c[k] ? (c[k - 1] ? g[k - 1] : cg) : g[k];
+      i[k] = c[k] ? (c[k - 1] ? i[k - 1] : ci) : i[k];
     }
-    return ct != __int_as_float(0x7f800000);
+    t[0] = c[0] ? ct : t[0];
+    g[0] = c[0] ? cg : g[0];
+    i[0] = c[0] ? ci : i[0];
+    return out != __int_as_float(0x7f800000);
   }
 };
 
