@@ -397,10 +397,20 @@ struct HitBuf {
 constexpr int kStack = KDGR_FAST_STACK;  // short-stack ring entries (ring + root restart as the reference)
 
 // Per-lane ray state; one leaf is processed per call of leaf_step.
+// The colour and depth accumulators of this thread's ray (r, g, b, depth),
+// in shared memory: they change only when a hit is blended and are read
+// once when the pixel is stored, so keeping them out of registers through
+// the candidate loop and the descent leaves those loops fewer spills
+// (64-register cap).
+__device__ __forceinline__ float4* acc_slot() {
+  __shared__ float4 s_acc[kThreads];
+  return &s_acc[threadIdx.x];
+}
+
 struct Ray {
   F3 o, d, inv;
   float t_near, t_far, t_scene_far;
-  float r, g, b, A, D;
+  float A;  // opacity; colour and depth accumulate in acc_slot()
   uint32_t cur, steps;
   unsigned top, quant;
 };
@@ -420,7 +430,8 @@ __device__ __forceinline__ bool ray_init(const FastView& S, const CamInfo& C, in
   const float il = rsqrtf(dot3(d, d));
   R.d = mk(d.x * il, d.y * il, d.z * il);
   R.inv = mk(1.f / R.d.x, 1.f / R.d.y, 1.f / R.d.z);
-  R.r = R.g = R.b = R.A = R.D = 0.f;
+  R.A = 0.f;
+  *acc_slot() = make_float4(0.f, 0.f, 0.f, 0.f);
   float tmin = 1e-2f, tmax = FLT_MAX;
   const float oo[3] = {R.o.x, R.o.y, R.o.z}, iv[3] = {R.inv.x, R.inv.y, R.inv.z};
 #pragma unroll
@@ -514,10 +525,13 @@ __device__ __forceinline__ void blend_hit(const FastView& S, Ray& R, float t, fl
   if (gres < 0.0113f || alpha < 1.0f / 255.0f) return;
   const F3 c = eval_sh_fast<PACKED>(S, gid, R.d);
   const float w = alpha * (1.f - R.A);
-  R.r = fmaf(c.x, w, R.r);
-  R.g = fmaf(c.y, w, R.g);
-  R.b = fmaf(c.z, w, R.b);
-  R.D = fmaf(t, w, R.D);
+  float4* acc = acc_slot();
+  float4 v = *acc;
+  v.x = fmaf(c.x, w, v.x);
+  v.y = fmaf(c.y, w, v.y);
+  v.z = fmaf(c.z, w, v.z);
+  v.w = fmaf(t, w, v.w);
+  *acc = v;
   R.A += w;
 }
 
@@ -843,11 +857,12 @@ __device__ __forceinline__ void store_px(const ViewDesc& V, int x, int y, const 
                                          float* depth_out) {
   const int W = __ldg(&V.W), H = __ldg(&V.H);
   const size_t idx = (size_t)__ldg(&V.out_off) + (size_t)(H - 1 - y) * W + x;  // rows flipped per view
-  rgb[3 * idx] = R.r;
-  rgb[3 * idx + 1] = R.g;
-  rgb[3 * idx + 2] = R.b;
+  const float4 v = *acc_slot();
+  rgb[3 * idx] = v.x;
+  rgb[3 * idx + 1] = v.y;
+  rgb[3 * idx + 2] = v.z;
   if (alpha_out) alpha_out[idx] = R.A;
-  if (depth_out) depth_out[idx] = R.D;
+  if (depth_out) depth_out[idx] = v.w;
 }
 
 // Render the ray of pixel (x, y) of view V to completion and store it.
