@@ -26,6 +26,10 @@ Every render line carries `accuracy`: max and RMS RGB error of the batched
 frame and of the plain kernel against the FP64 oracle on a ray sample, and
 the plain kernel against the oracle-matching FP32 oracle (expected 0).
 
+The batched configuration is the autotuner's (kdgr_autotune), re-ranked:
+its three fastest variants are timed again under the timed region's
+conditions (L2 flushed before each step) and the fastest is used
+(`autotune_reranked` lists both times).
 `value` is the batched (persistent, CUDA-graph) form with the scene resident
 in HBM, timed with CUDA events per step with an L2 flush (a 512 MB write)
 between steps.  `e2e` is the same metric through the C ABI
@@ -273,6 +277,44 @@ def wall_loop(step_fn, k, flush, dev):
     return out
 
 
+def rerank(F, scene, views, n_views, rgb, cfg, report, flush, stream, dev, top: int = 3):
+    """The autotuner ranks its variants back to back, with the scene's working
+    set warm in L2 (as in a frame loop); the timed region flushes L2 before
+    every step.  Re-time the autotuner's `top` fastest configurations under
+    the timed region's conditions (flush, then the graph replay) and return
+    the fastest, with every time."""
+    rows = []
+    for line in report.splitlines():
+        try:
+            d = json.loads(line)
+        except ValueError:
+            continue
+        if isinstance(d, dict) and "ms" in d:
+            rows.append(d)
+    rows.sort(key=lambda d: d["ms"])
+    best, best_ms, tried, seen = cfg, None, [], set()
+    for d in rows:
+        key = tuple(sorted((k, v) for k, v in d.items() if k != "ms"))
+        if key in seen:
+            continue
+        seen.add(key)
+        c = F.BatchConfig.default()
+        for k, v in d.items():
+            if k != "ms":
+                setattr(c, k, v)
+        b = F.Batch(scene, views, n_views, rgb, None, None, c)
+        for _ in range(2):
+            b.run()
+        ms = statistics.median(timed_loop(b.run, 5, flush, stream, dev))
+        b.close()
+        tried.append({**{k: v for k, v in d.items() if k != "ms"}, "warm_ms": d["ms"], "flushed_ms": round(ms, 4)})
+        if best_ms is None or ms < best_ms:
+            best, best_ms = c, ms
+        if len(seen) >= top:
+            break
+    return best, tried
+
+
 def run_ours(args, rank: int, world: int):
     import torch
     pkg = importlib.import_module(PKG)
@@ -293,14 +335,19 @@ def run_ours(args, rank: int, world: int):
     views, total_px, offs = F.make_views(cams)
     rays = desc["rays_per_step"]
     rgb = torch.zeros(total_px * 3, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
     # autotuned persistent-kernel configuration
+    reranked = None
     if args.profile:
         cfg = F.BatchConfig.default()
         cfg.precision = precision
     else:
         cfg, report = scene.autotune(views, len(cams), rgb, precision=precision)
         log("[bench] autotuner variants:\n" + report.strip())
-        log(f"[bench] autotuner picked {cfg.as_dict()}")
+        cfg, reranked = rerank(F, scene, views, len(cams), rgb, cfg, report, flush, stream, dev)
+        log(f"[bench] autotuner's three fastest re-timed with the L2 flush: {reranked}")
+        log(f"[bench] picked {cfg.as_dict()}")
     batch = F.Batch(scene, views, len(cams), rgb, None, None, cfg)
     if args.profile:
         for _ in range(args.warmup + args.steps):
@@ -312,8 +359,6 @@ def run_ours(args, rank: int, world: int):
         assert scene.status() == 0
         print(json.dumps({"profile_run": args.config, "launches": args.warmup + args.steps}), flush=True)
         raise SystemExit(0)
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    stream = torch.cuda.current_stream(dev)
 
     clocks = ClockSampler(dev.index)
     for _ in range(args.warmup):
@@ -396,6 +441,7 @@ def run_ours(args, rank: int, world: int):
         "dtype": "bf16/fp16 storage, fp32 arithmetic" if precision else "f32", "data": "synthetic",
         "config": common_config(desc, world),
         "form": "batched persistent kernel, CUDA graph", "autotuned": cfg.as_dict(),
+        "autotune_reranked": reranked,
         "e2e": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in e2e.items()},
         "roofline": roofline(f"{args.config}:{'packed' if precision else 'fp32'}", ms_step, clk, sms, alg_bytes,
                              rays),
@@ -448,7 +494,8 @@ def leg_batching(pkg, scene, tree, rec, dev, flush, stream, args, check: bool):
     views, total, offs = F.make_views(cams)
     rays = int(sum(w * h for _, w, h in cams))
     rgb = torch.zeros(total * 3, device=dev)
-    cfg, _ = scene.autotune(views, len(cams), rgb, precision=0)
+    cfg, report = scene.autotune(views, len(cams), rgb, precision=0)
+    cfg, _ = rerank(F, scene, views, len(cams), rgb, cfg, report, flush, stream, dev)
     batch = F.Batch(scene, views, len(cams), rgb, None, None, cfg)
     for _ in range(2):
         batch.run()
