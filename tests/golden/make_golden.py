@@ -1,5 +1,5 @@
 """Generate the committed golden fixtures (run in a tree where the reference
-sources are present; the GPU machine only reads the outputs).
+sources are present; machines without them only read the outputs).
 
 For each fixture scene:
   * <name>.scene.npy  -- activated Gaussian records (n, 64) float32;
